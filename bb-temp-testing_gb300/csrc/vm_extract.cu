@@ -1,0 +1,273 @@
+// Voronoi cell clipping for mesh extraction (reference voronoiCellKernel,
+// voro_optimizer.cu:312-437).
+//
+// Per generator: the 32 nearest sites by ring search, then the domain box is
+// clipped (Sutherland-Hodgman, the reference's vertex/edge-label bookkeeping)
+// by the bisectors of those neighbours in kNN order until the security radius
+// certifies the cell (|cj - ci|^2 > 4 max|v - ci|^2); an uncertified cell
+// falls back to every generator in index order, as in the reference.
+//
+// Arithmetic: each polygon vertex is the intersection of the lines of its two
+// edges, solved once in FP64 by a 2x2 determinant when the vertex is created
+// and kept in FP64 (and rounded to FP32). The inside/outside test of a vertex
+// against a new bisector runs in FP32 with a rigorous error bound and is
+// re-evaluated in FP64 only when the FP32 value lies inside that bound.
+// Centroid and output vertices use the FP64 vertices, as the reference does.
+#include "vm_device.cuh"
+#include "vm_kernels.h"
+#include "vm_knn.cuh"
+
+namespace vmk {
+
+constexpr int kMaxVerts = 24;
+constexpr int kCellK = 32;
+
+struct CellPoly {
+    double vx[kMaxVerts], vy[kMaxVerts];
+    float fx[kMaxVerts], fy[kMaxVerts];
+    int lab[kMaxVerts];
+    int n;
+};
+
+struct CellCtx {
+    float2 ci;
+    double w, h; // domain size
+    const float2 *gen;
+};
+
+// Line of an edge label in coordinates relative to ci: a . x = b.
+// label >= 0: bisector of ci and gen[label]; -1..-4: top, right, bottom, left box side.
+__device__ __forceinline__ void line_of(const CellCtx &c, int L, double &ax, double &ay, double &b)
+{
+    if (L >= 0) {
+        float2 g = c.gen[L];
+        double rx = (double)g.x - (double)c.ci.x, ry = (double)g.y - (double)c.ci.y;
+        ax = rx;
+        ay = ry;
+        b = 0.5 * (rx * rx + ry * ry);
+    } else if (L == -1) {
+        ax = 0.0; ay = 1.0; b = -(double)c.ci.y;
+    } else if (L == -2) {
+        ax = 1.0; ay = 0.0; b = c.w - (double)c.ci.x;
+    } else if (L == -3) {
+        ax = 0.0; ay = 1.0; b = c.h - (double)c.ci.y;
+    } else {
+        ax = 1.0; ay = 0.0; b = -(double)c.ci.x;
+    }
+}
+
+// Intersection of the line of label L with the bisector (rx, ry, cc).
+__device__ __forceinline__ void intersect(const CellCtx &c, int L, double rx, double ry, double cc, double fbx,
+                                          double fby, double &x, double &y)
+{
+    double ax, ay, b;
+    line_of(c, L, ax, ay, b);
+    double det = ax * ry - ay * rx;
+    if (det == 0.0) { // parallel: keep the edge point (cannot happen for a proper crossing)
+        x = fbx;
+        y = fby;
+        return;
+    }
+    x = (b * ry - cc * ay) / det;
+    y = (ax * cc - rx * b) / det;
+}
+
+// 1 if vertex k is outside the half-plane <x, r> <= |r|^2/2 (reference clipByBisector :322-325)
+__device__ __forceinline__ bool outside(const CellPoly &P, int k, float rfx, float rfy, float cf, double rx, double ry,
+                                        double cc)
+{
+    float a = P.fx[k] * rfx, b = P.fy[k] * rfy;
+    float f = a + b - cf;
+    float bound = 1.9073486328125e-06f * (fabsf(a) + fabsf(b) + cf + fabsf(f)) + 1e-37f; // 2^-19
+    if (f > bound) return true;
+    if (f < -bound) return false;
+    return P.vx[k] * rx + P.vy[k] * ry - cc > 0.0;
+}
+
+// Clip P by the bisector of ci and site j (reference clipByBisector :320-351).
+// Writes into Q; returns false on vertex overflow. *changed = 0 if no vertex was outside.
+__device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, float2 cj, bool &changed)
+{
+    double rx = (double)cj.x - (double)c.ci.x, ry = (double)cj.y - (double)c.ci.y;
+    double cc = 0.5 * (rx * rx + ry * ry);
+    float rfx = (float)rx, rfy = (float)ry;
+    float cf = 0.5f * (rfx * rfx + rfy * rfy);
+    unsigned out = 0;
+    for (int k = 0; k < P.n; ++k)
+        if (outside(P, k, rfx, rfy, cf, rx, ry, cc)) out |= 1u << k;
+    if (!out) {
+        changed = false;
+        return true;
+    }
+    changed = true;
+    bool ok = true;
+    Q.n = 0;
+    for (int k = 0; k < P.n; ++k) {
+        int k1 = k + 1 == P.n ? 0 : k + 1;
+        bool inA = !((out >> k) & 1u), inB = !((out >> k1) & 1u);
+        if (inA) {
+            if (Q.n < kMaxVerts) {
+                Q.vx[Q.n] = P.vx[k]; Q.vy[Q.n] = P.vy[k];
+                Q.fx[Q.n] = P.fx[k]; Q.fy[Q.n] = P.fy[k];
+                Q.lab[Q.n] = P.lab[k];
+                ++Q.n;
+            } else ok = false;
+        }
+        if (inA != inB) {
+            double x, y;
+            intersect(c, P.lab[k], rx, ry, cc, P.vx[k], P.vy[k], x, y);
+            if (Q.n < kMaxVerts) {
+                Q.vx[Q.n] = x; Q.vy[Q.n] = y;
+                Q.fx[Q.n] = (float)x; Q.fy[Q.n] = (float)y;
+                Q.lab[Q.n] = inA ? j : P.lab[k];
+                ++Q.n;
+            } else ok = false;
+        }
+    }
+    return ok;
+}
+
+__device__ __forceinline__ float r2max_f(const CellPoly &P)
+{
+    float r = 0.0f;
+    for (int k = 0; k < P.n; ++k) r = fmaxf(r, P.fx[k] * P.fx[k] + P.fy[k] * P.fy[k]);
+    return r;
+}
+
+__device__ __forceinline__ double r2max_d(const CellPoly &P)
+{
+    double r = 0.0;
+    for (int k = 0; k < P.n; ++k) r = fmax(r, P.vx[k] * P.vx[k] + P.vy[k] * P.vy[k]);
+    return r;
+}
+
+// (double)dd > 4 * maxRadius2(P), decided in FP32 unless within its error band.
+__device__ __forceinline__ bool beyond(float dd, const CellPoly &P)
+{
+    float r = 4.0f * r2max_f(P);
+    if (dd > r * 1.0000038146972656f) return true;  // 1 + 2^-18
+    if (dd < r * 0.9999961853027344f) return false; // 1 - 2^-18
+    return (double)dd > 4.0 * r2max_d(P);
+}
+
+__device__ __forceinline__ bool occupied(const unsigned long long *masks, int tilesX, int tilesY, float invVoxel,
+                                         float2 p)
+{
+    if (!masks) return false;
+    float fx = floorf(p.x * invVoxel), fy = floorf(p.y * invVoxel);
+    if (!(fx >= 0.0f) || !(fy >= 0.0f) || fx >= 2147483647.0f || fy >= 2147483647.0f) return false;
+    int i = (int)fx, j = (int)fy;
+    int tx = i >> 3, ty = j >> 3;
+    if (tx >= tilesX || ty >= tilesY) return false;
+    return (masks[(size_t)ty * tilesX + tx] >> (((j & 7) << 3) | (i & 7))) & 1ull;
+}
+
+__global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, const unsigned long long *masks,
+                                               int tilesX, int tilesY, float invVoxel, float2 *__restrict__ outVerts,
+                                               int *__restrict__ outEdges, int *__restrict__ outCount,
+                                               unsigned char *__restrict__ outInside, int *__restrict__ flags)
+{
+    const VmFit &F = *fit;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.nSlots) return;
+    float2 ci = F.gen[i];
+    if (ci.x < 0.0f) {
+        outCount[i] = 0;
+        outInside[i] = 0;
+        return;
+    }
+    float d2[kCellK];
+    int idx[kCellK];
+    knn_ring<kCellK>(F.start, F.sortedPos, F.sortedIdx, F.gridW, F.gridH, F.cell, F.inv, ci, d2, idx);
+
+    CellCtx c;
+    c.ci = ci;
+    c.w = (double)F.width;
+    c.h = (double)F.height;
+    c.gen = F.gen;
+    CellPoly buf[2];
+    CellPoly *P = &buf[0], *Q = &buf[1];
+    double x0 = -(double)ci.x, y0 = -(double)ci.y, x1 = c.w - (double)ci.x, y1 = c.h - (double)ci.y;
+    P->vx[0] = x0; P->vy[0] = y0; P->lab[0] = -1;
+    P->vx[1] = x1; P->vy[1] = y0; P->lab[1] = -2;
+    P->vx[2] = x1; P->vy[2] = y1; P->lab[2] = -3;
+    P->vx[3] = x0; P->vy[3] = y1; P->lab[3] = -4;
+    for (int k = 0; k < 4; ++k) {
+        P->fx[k] = (float)P->vx[k];
+        P->fy[k] = (float)P->vy[k];
+    }
+    P->n = 4;
+
+    bool ok = true, certified = false;
+    for (int k = 0; k < kCellK; ++k) {
+        int j = idx[k];
+        if (j < 0) {
+            certified = true; // every generator has been seen
+            break;
+        }
+        if (j == i) continue;
+        if (beyond(d2[k], *P)) {
+            certified = true;
+            break;
+        }
+        bool changed;
+        ok &= clip(c, *P, *Q, j, F.gen[j], changed);
+        if (changed) {
+            CellPoly *t = P; P = Q; Q = t;
+        }
+    }
+    if (!certified && beyond(d2[kCellK - 1], *P)) certified = true;
+    if (!certified) {
+        atomicAdd(&flags[0], 1);
+        for (int j = 0; j < F.nSlots; ++j) {
+            if (j == i) continue;
+            float2 g = F.gen[j];
+            if (g.x < 0.0f) continue;
+            bool seen = false;
+            for (int k = 0; k < kCellK; ++k) seen |= idx[k] == j;
+            if (seen) continue;
+            double rx = (double)g.x - (double)ci.x, ry = (double)g.y - (double)ci.y;
+            if (rx * rx + ry * ry > 4.0 * r2max_d(*P)) continue;
+            bool changed;
+            ok &= clip(c, *P, *Q, j, g, changed);
+            if (changed) {
+                CellPoly *t = P; P = Q; Q = t;
+            }
+        }
+    }
+    if (!ok) atomicAdd(&flags[1], 1);
+
+    // centroid (shoelace) -> occupancy (reference :417-431)
+    double area = 0.0, cx = 0.0, cy = 0.0;
+    for (int k = 0; k < P->n; ++k) {
+        int k1 = k + 1 == P->n ? 0 : k + 1;
+        double ax = P->vx[k], ay = P->vy[k], bx = P->vx[k1], by = P->vy[k1];
+        double cr = ax * by - bx * ay;
+        area += cr;
+        cx += (ax + bx) * cr;
+        cy += (ay + by) * cr;
+    }
+    float2 centroid = ci;
+    if (fabs(area) > 1e-12) {
+        centroid.x += (float)(cx / (3.0 * area));
+        centroid.y += (float)(cy / (3.0 * area));
+    }
+    outInside[i] = occupied(masks, tilesX, tilesY, invVoxel, centroid) ? 1 : 0;
+    outCount[i] = P->n;
+    for (int k = 0; k < P->n; ++k) {
+        outVerts[(size_t)i * kMaxVerts + k] = make_float2((float)((double)ci.x + P->vx[k]), (float)((double)ci.y + P->vy[k]));
+        outEdges[(size_t)i * kMaxVerts + k] = P->lab[k];
+    }
+}
+
+} // namespace vmk
+
+cudaError_t vm_launch_cells_n(const VmFit *fit, int nSlots, const unsigned long long *masks, int tilesX, int tilesY,
+                              float invVoxel, float2 *outVerts, int *outEdges, int *outCount,
+                              unsigned char *outInside, int *flags, cudaStream_t s)
+{
+    if (nSlots <= 0) return cudaSuccess;
+    vmk::k_cells<<<(nSlots + 127) / 128, 128, 0, s>>>(fit, masks, tilesX, tilesY, invVoxel, outVerts, outEdges,
+                                                      outCount, outInside, flags);
+    return cudaGetLastError();
+}

@@ -1,0 +1,67 @@
+// Host-side helpers shared by the runtime translation units (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "vm_capi.h"
+#include "vm_types.h"
+
+namespace vmh {
+
+constexpr int kMaxCellVerts = 24;
+
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+int floor_log2f(float h);
+
+// Owning device buffer. alloc() replaces the contents; reserve() keeps the
+// buffer when it is already large enough.
+template <class T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    int alloc(size_t count)
+    {
+        release();
+        if (count == 0) return VM_OK;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e) {
+            p = nullptr;
+            return cuda_fail(e, "cudaMalloc");
+        }
+        n = count;
+        return VM_OK;
+    }
+    int reserve(size_t count) { return count <= n && p ? VM_OK : alloc(count); }
+};
+
+struct MeshHost {
+    std::vector<float2> generators;
+    std::vector<uint8_t> inside;
+    std::vector<int> cellStart;
+    std::vector<float2> cellVerts;
+    std::vector<int> cellLabels;
+    std::vector<float2> vertices;
+    std::vector<int> edges; // pairs
+    bool watertight = false;
+    int loops = 0, unsafeCells = 0, overflowCells = 0;
+    float gpuMs = 0.0f, hostMs = 0.0f;
+};
+
+void assemble_boundary(const std::vector<float2> &verts, const std::vector<int> &labels,
+                       const std::vector<int> &counts, const std::vector<uint8_t> &inside, int n, MeshHost &mesh);
+
+} // namespace vmh

@@ -1,0 +1,44 @@
+// Host-side launch wrappers of the VoroMesh kernels (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "vm_types.h"
+
+cudaError_t vm_launch_bin(const VmPointSet *sets, const int *prefix, int nSets, int totalBlocks, int emptyIsNegative,
+                          cudaStream_t s);
+cudaError_t vm_launch_scan(const VmPointSet *sets, const int *tilePrefix, int nSets, int totalTiles, cudaStream_t s);
+cudaError_t vm_launch_scatter(const VmPointSet *sets, const int *prefix, int nSets, int totalBlocks,
+                              const VmFit *publish, cudaStream_t s);
+// The loss pass is two launches: the block-certified fast path over all
+// targets, then the exact ring search over the targets it deferred to the
+// queue (created by vm_queue_init; items hold (fit, target) int2 pairs).
+// `variant` picks block size, occupancy target and gradient aggregation; its
+// block size is also the number of targets per tile the prefix table counts.
+cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode, int maxR,
+                           int gridBlocks, int variant, void *queue, cudaStream_t s);
+int vm_loss_variants();
+int vm_loss_variant_threads(int variant);
+cudaError_t vm_launch_finalize(const VmFit *fits, int nFits, void *queue, cudaStream_t s);
+cudaError_t vm_launch_adam_bin(const VmFit *fits, const int *prefix, int nFits, int totalBlocks, void *queue,
+                               cudaStream_t s);
+cudaError_t vm_queue_init(void *queue, void *items, int capacity, cudaStream_t s);
+size_t vm_queue_bytes();
+cudaError_t vm_launch_knn(const VmFit *fit, const float2 *q, int nq, int K, int *outIdx, float *outD2,
+                          cudaStream_t s);
+int vm_loss_occupancy_blocks(int variant);
+cudaError_t vm_launch_scatter_targets(float2 *targets, const int *slots, const float2 *values, int n, cudaStream_t s);
+
+// Voronoi cells for extraction (vm_extract.cu)
+cudaError_t vm_launch_cells_n(const VmFit *fit, int nSlots, const unsigned long long *masks, int tilesX, int tilesY,
+                              float invVoxel, float2 *outVerts, int *outEdges, int *outCount,
+                              unsigned char *outInside, int *flags, cudaStream_t s);
+
+// Poisson phase-grid sampler (vm_poisson.cu)
+struct PdParams {
+    float width, height, radius, cellSize;
+    int gridW, gridH;
+    unsigned seed;
+};
+cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int trials,
+                               unsigned roundBase, cudaStream_t s);

@@ -1,0 +1,89 @@
+// Phase-grid parallel Poisson-disk dart throwing (reference poisson_disk.cu:74-177,
+// after Wei 2008).
+//
+// The background grid has cell size r/sqrt(2), so a cell holds at most one
+// sample and a dart can only conflict with the 5x5 block around its cell.
+// Cells are coloured by (x mod 3, y mod 3) relative to the region origin;
+// cells of one colour are >= 3 apart and never see each other's writes, so a
+// colour phase is race-free. Each round runs the 9 phases in the reference's
+// order (py outer, px inner) and draws darts from a stateless hash of
+// (cell, round, seed), which makes the sample set a deterministic function of
+// the inputs and the sequence of regions resampled.
+//
+// Each phase is one launch over the phase cells of the region.
+#include "vm_device.cuh"
+#include "vm_kernels.h"
+
+namespace vmk {
+
+__device__ __forceinline__ float prand01(unsigned cell, unsigned round, unsigned seed, unsigned stream)
+{
+    unsigned h = pcg_hash(cell ^ pcg_hash(round * 2654435761u ^ pcg_hash(seed + stream * 0x9E3779B9u)));
+    return (float)(h & 0x00FFFFFFu) * (1.0f / 16777216.0f);
+}
+
+// One dart for cell (cx, cy) (reference dartPhaseKernel :84-106).
+__device__ __forceinline__ void dart(float2 *grid, const PdParams &p, int cx, int cy, unsigned round)
+{
+    int cellId = cy * p.gridW + cx;
+    if (grid[cellId].x >= 0.0f) return;
+    float x = ((float)cx + prand01((unsigned)cellId, round, p.seed, 0u)) * p.cellSize;
+    float y = ((float)cy + prand01((unsigned)cellId, round, p.seed, 1u)) * p.cellSize;
+    if (x >= p.width || y >= p.height) return;
+    float r2 = p.radius * p.radius;
+    int x0 = max(cx - 2, 0), x1 = min(cx + 2, p.gridW - 1);
+    int y0 = max(cy - 2, 0), y1 = min(cy + 2, p.gridH - 1);
+    for (int ny = y0; ny <= y1; ++ny)
+        for (int nx = x0; nx <= x1; ++nx) {
+            float2 q = grid[ny * p.gridW + nx];
+            if (q.x < 0.0f) continue;
+            float dx = q.x - x, dy = q.y - y;
+            if (dx * dx + dy * dy < r2) return;
+        }
+    grid[cellId] = make_float2(x, y);
+}
+
+__global__ void __launch_bounds__(256) k_clear(float2 *grid, int gridW, int x0, int y0, int x1, int y1)
+{
+    int rw = x1 - x0;
+    long long n = (long long)rw * (y1 - y0);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int cx = x0 + (int)(t % rw), cy = y0 + (int)(t / rw);
+        grid[(size_t)cy * gridW + cx] = make_float2(-1.0f, -1.0f);
+    }
+}
+
+// One phase (px, py) of one round, one thread per phase cell.
+__global__ void __launch_bounds__(256) k_phase(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int px,
+                                               int py, unsigned round)
+{
+    int tw = (x1 - x0 - px + 2) / 3, th = (y1 - y0 - py + 2) / 3;
+    long long n = (long long)tw * th;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int tx = (int)(t % tw), ty = (int)(t / tw);
+        dart(grid, p, x0 + 3 * tx + px, y0 + 3 * ty + py, round);
+    }
+}
+
+} // namespace vmk
+
+using namespace vmk;
+
+cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int trials,
+                               unsigned roundBase, cudaStream_t s)
+{
+    int rw = x1 - x0, rh = y1 - y0;
+    if (rw <= 0 || rh <= 0) return cudaSuccess;
+    long long cells = (long long)rw * rh;
+    int cb = (int)((cells + 255) / 256);
+    if (cb > 65535) cb = 65535;
+    k_clear<<<cb, 256, 0, s>>>(grid, p.gridW, x0, y0, x1, y1);
+    long long phaseCells = ((long long)(rw + 2) / 3) * ((rh + 2) / 3);
+    int pb = (int)((phaseCells + 255) / 256);
+    if (pb > 65535) pb = 65535;
+    for (int round = 0; round < trials; ++round)
+        for (int py = 0; py < 3; ++py)
+            for (int px = 0; px < 3; ++px)
+                k_phase<<<pb, 256, 0, s>>>(grid, p, x0, y0, x1, y1, px, py, roundBase + (unsigned)round);
+    return cudaGetLastError();
+}

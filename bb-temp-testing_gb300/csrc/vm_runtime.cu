@@ -1,0 +1,1073 @@
+// Host runtime of the single-fit optimiser and the Poisson sampler behind the
+// C ABI (include/vm_capi.h). Each function mirrors one method of the
+// reference's VoroOptimizer / Sampler (src/voromesh/voro_optimizer.cu:512-858,
+// src/poisson/poisson_disk.cu:119-199); the device work is the batch-native
+// kernels of vm_step.cu / vm_extract.cu / vm_poisson.cu run on a batch of one.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "vm_capi.h"
+#include "vm_host.h"
+#include "vm_kernels.h"
+
+namespace vmh {
+
+thread_local std::string g_lastError;
+
+int fail(int code, const std::string &msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    int code = e == cudaErrorMemoryAllocation ? VM_ERR_OOM
+               : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? VM_ERR_NODEVICE
+                                                                              : VM_ERR_CUDA;
+    return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int floor_log2f(float h)
+{
+    int e = 0;
+    std::frexp(h, &e);
+    return e - 1;
+}
+
+// Boundary assembly of Extract() (reference voro_optimizer.cu:798-854).
+void assemble_boundary(const std::vector<float2> &verts, const std::vector<int> &labels,
+                       const std::vector<int> &counts, const std::vector<uint8_t> &inside, int n, MeshHost &mesh)
+{
+    mesh.cellStart.assign((size_t)n + 1, 0);
+    for (int i = 0; i < n; ++i) mesh.cellStart[i + 1] = mesh.cellStart[i] + counts[i];
+    mesh.cellVerts.resize((size_t)mesh.cellStart[n]);
+    mesh.cellLabels.resize((size_t)mesh.cellStart[n]);
+    for (int i = 0; i < n; ++i) {
+        std::copy_n(verts.begin() + (size_t)i * kMaxCellVerts, counts[i], mesh.cellVerts.begin() + mesh.cellStart[i]);
+        std::copy_n(labels.begin() + (size_t)i * kMaxCellVerts, counts[i], mesh.cellLabels.begin() + mesh.cellStart[i]);
+    }
+    // vertex key: the sorted generator triple (labels offset by the 4 box sides, 21 bits each)
+    auto key = [](int a, int b, int c) {
+        uint64_t v0 = uint64_t(a + 4), v1 = uint64_t(b + 4), v2 = uint64_t(c + 4);
+        if (v0 > v1) std::swap(v0, v1);
+        if (v1 > v2) std::swap(v1, v2);
+        if (v0 > v1) std::swap(v0, v1);
+        return (v0 << 42) | (v1 << 21) | v2;
+    };
+    size_t maxEdges = 0;
+    for (int i = 0; i < n; ++i)
+        if (inside[i]) maxEdges += (size_t)counts[i];
+    size_t cap = 64;
+    while (cap < 4 * (maxEdges + 16)) cap <<= 1;
+    std::vector<uint64_t> keys(cap);
+    std::vector<int> vals(cap, -1);
+    auto vertex = [&](uint64_t k, float2 p) {
+        uint64_t h = k;
+        h ^= h >> 33; h *= 0xff51afd7ed558ccdULL; h ^= h >> 33; h *= 0xc4ceb9fe1a85ec53ULL; h ^= h >> 33;
+        size_t s = (size_t)h & (cap - 1);
+        while (vals[s] >= 0) {
+            if (keys[s] == k) return vals[s];
+            s = (s + 1) & (cap - 1);
+        }
+        keys[s] = k;
+        vals[s] = (int)mesh.vertices.size();
+        mesh.vertices.push_back(p);
+        return vals[s];
+    };
+    mesh.vertices.clear();
+    mesh.edges.clear();
+    for (int i = 0; i < n; ++i) {
+        if (!inside[i]) continue;
+        int c = counts[i];
+        const int *lab = labels.data() + (size_t)i * kMaxCellVerts;
+        const float2 *pos = verts.data() + (size_t)i * kMaxCellVerts;
+        for (int k = 0; k < c; ++k) {
+            int l = lab[k];
+            if (l >= 0 && inside[l]) continue;
+            int prev = lab[(k + c - 1) % c], next = lab[(k + 1) % c];
+            int a = vertex(key(i, prev, l), pos[k]);
+            int b = vertex(key(i, l, next), pos[(k + 1) % c]);
+            mesh.edges.push_back(a);
+            mesh.edges.push_back(b);
+        }
+    }
+    size_t nv = mesh.vertices.size(), ne = mesh.edges.size() / 2;
+    std::vector<int> nxt(nv, -1), inDeg(nv, 0);
+    mesh.watertight = true;
+    mesh.loops = 0;
+    for (size_t e = 0; e < ne; ++e) {
+        int a = mesh.edges[2 * e], b = mesh.edges[2 * e + 1];
+        if (nxt[a] != -1) mesh.watertight = false;
+        nxt[a] = b;
+        ++inDeg[b];
+    }
+    for (size_t v = 0; v < nv; ++v)
+        if (nxt[v] == -1 || inDeg[v] != 1) mesh.watertight = false;
+    if (mesh.watertight) {
+        std::vector<uint8_t> seen(nv, 0);
+        for (size_t v = 0; v < nv; ++v) {
+            if (seen[v]) continue;
+            ++mesh.loops;
+            for (int w = (int)v; !seen[w]; w = nxt[w]) seen[w] = 1;
+        }
+    }
+}
+
+} // namespace vmh
+
+using namespace vmh;
+
+// ===========================================================================
+// optimiser handle
+// ===========================================================================
+struct vm_optimizer {
+    float width = 0, height = 0, spacing = 0;
+    vm_params params{};
+    int gridW = 0, gridH = 0, cells = 0, tiles = 0;
+    int slotsW = 0, slotsH = 0;
+    float slotCellSize = 0;
+    int targetCapacity = 0, liveTargets = 0;
+    int iteration = 0, scheduleLength = 0;
+    float lastBatchLoss = 0;
+    bool gridValid = false;
+    int lossGrid = 0;
+    int lossTile = 256;    // targets per loss tile (= its block size)
+    int lossVariant = 3;   // loss kernel variant in use
+    int lossForced = -1;   // variant chosen by the caller (vm_set_loss_variant), -1 = automatic
+
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t graph = nullptr;
+
+    DevBuf<float2> gen, m, v, sortedPos, traw, tpos, stageVals, qbuf, cellVerts;
+    DevBuf<long long> gradX;
+    DevBuf<int> key, rank, counts, start, tileSums, sortedIdx, tkey, trank, tslot, stageSlots, kIdx, cellEdges,
+        cellCount, flags, dbgI0, dbgJ;
+    DevBuf<float> kD2, dbgLoss;
+    DevBuf<unsigned char> inside;
+    DevBuf<unsigned long long> occ;
+    DevBuf<VmState> state;
+    DevBuf<VmFit> dFit;
+    DevBuf<VmPointSet> dSites, dTargets;
+    DevBuf<int> dPre; // [0, siteBlocks, 0, tiles, 0, lossTiles, 0, targetBlocks]
+    DevBuf<char> queue;  // deferred-target queue header
+    DevBuf<int2> qitems; // its items
+    std::vector<cudaEvent_t> timing; // vm_step_timed events
+    int tilesX = 0, tilesY = 0;
+    float invVoxel = 0;
+    VmFit fit{};
+    MeshHost mesh;
+    long long exactTotal = 0;
+
+    int numSlots() const { return slotsW * slotsH; }
+};
+
+namespace {
+
+int upload_tables(vm_optimizer *h)
+{
+    VmFit &F = h->fit;
+    int n = h->numSlots();
+    F.nSlots = n;
+    F.slotsW = h->slotsW;
+    F.slotsH = h->slotsH;
+    F.gridW = h->gridW;
+    F.gridH = h->gridH;
+    F.cell = h->spacing;
+    F.inv = 1.0f / h->spacing;
+    F.width = h->width;
+    F.height = h->height;
+    F.K = h->params.lossK;
+    F.fraction = h->params.sampleFraction;
+    F.seed = h->params.seed;
+    F.gradExp = 40 - floor_log2f(h->spacing);
+    F.lossExp = 64 - 2 * floor_log2f(h->spacing);
+    F.nTargets = h->liveTargets;
+    F.active = 1;
+    F.gen = h->gen.p; F.m = h->m.p; F.v = h->v.p; F.gradX = h->gradX.p;
+    F.key = h->key.p; F.rank = h->rank.p; F.counts = h->counts.p; F.start = h->start.p; F.tileSums = h->tileSums.p;
+    F.sortedIdx = h->sortedIdx.p; F.sortedPos = h->sortedPos.p;
+    F.tpos = h->tpos.p; F.tslot = h->tslot.p;
+    F.state = h->state.p;
+    VmPointSet S{};
+    S.pts = h->gen.p; S.n = n; S.gridW = h->gridW; S.gridH = h->gridH; S.inv = F.inv;
+    S.key = h->key.p; S.rank = h->rank.p; S.counts = h->counts.p; S.start = h->start.p; S.tileSums = h->tileSums.p;
+    S.outPos = h->sortedPos.p; S.outIdx = h->sortedIdx.p; S.canonical = 1; S.useIndexOrder = 1;
+    VmPointSet T = S;
+    T.pts = h->traw.p; T.n = h->targetCapacity; T.key = h->tkey.p; T.rank = h->trank.p;
+    T.outPos = h->tpos.p; T.outIdx = h->tslot.p; T.canonical = 0;
+    int pre[8] = {0, (n + 255) / 256, 0, h->tiles, 0, (h->liveTargets + h->lossTile - 1) / h->lossTile, 0,
+                  (h->targetCapacity + 255) / 256};
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(h->dFit.p, &F, sizeof(VmFit), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload fit");
+    if ((e = cudaMemcpyAsync(h->dSites.p, &S, sizeof(S), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload sites");
+    if ((e = cudaMemcpyAsync(h->dTargets.p, &T, sizeof(T), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload targets");
+    if ((e = cudaMemcpyAsync(h->dPre.p, pre, sizeof(pre), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload prefix");
+    // the tables live in pageable memory on the host: finish before they change
+    if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "upload sync");
+    return VM_OK;
+}
+
+void drop_graph(vm_optimizer *h)
+{
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+}
+
+// Loss kernel variant: the caller's choice, else VM_LOSS_VARIANT, else 64-thread
+// tiles for small fits (more blocks in flight) and 256-thread tiles otherwise.
+void choose_loss_variant(vm_optimizer *h, int sms)
+{
+    int v = h->lossForced;
+    if (v < 0) {
+        const char *env = std::getenv("VM_LOSS_VARIANT");
+        if (env && *env) v = std::atoi(env);
+    }
+    if (v < 0 || v >= vm_loss_variants()) v = h->liveTargets < 256 * 4 * sms ? 7 : 3;
+    h->lossVariant = v;
+    h->lossTile = vm_loss_variant_threads(v);
+    h->lossGrid = vm_loss_occupancy_blocks(v);
+}
+
+int enqueue_build_grid(vm_optimizer *h)
+{
+    int n = h->numSlots();
+    cudaError_t e;
+    if ((e = vm_launch_bin(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, 1, h->stream))) return cuda_fail(e, "bin");
+    if ((e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "scan");
+    if ((e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, nullptr, h->stream)))
+        return cuda_fail(e, "scatter");
+    return VM_OK;
+}
+
+int ensure_grid(vm_optimizer *h)
+{
+    if (h->gridValid) return VM_OK;
+    int rc = enqueue_build_grid(h);
+    if (rc) return rc;
+    h->gridValid = true;
+    return VM_OK;
+}
+
+int enqueue_step(vm_optimizer *h)
+{
+    int n = h->numSlots();
+    cudaError_t e;
+    int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)))
+        return cuda_fail(e, "loss");
+    if ((e = vm_launch_adam_bin(h->dFit.p, h->dPre.p + 0, 1, (n + 255) / 256, h->queue.p, h->stream)))
+        return cuda_fail(e, "adam");
+    if ((e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "scan");
+    if ((e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, h->dFit.p, h->stream)))
+        return cuda_fail(e, "scatter");
+    return VM_OK;
+}
+
+int ensure_graph(vm_optimizer *h)
+{
+    if (h->graph) return VM_OK;
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e) return cuda_fail(e, "begin capture");
+    int rc = enqueue_step(h);
+    e = cudaStreamEndCapture(h->stream, &g);
+    if (rc) return rc;
+    if (e) return cuda_fail(e, "end capture");
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e) return cuda_fail(e, "graph instantiate");
+    return VM_OK;
+}
+
+int read_state(vm_optimizer *h, VmState &st)
+{
+    cudaError_t e = cudaMemcpyAsync(&st, h->state.p, sizeof(VmState), cudaMemcpyDeviceToHost, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cuda_fail(e, "read state");
+    return VM_OK;
+}
+
+int sort_targets(vm_optimizer *h)
+{
+    cudaError_t e;
+    int tb = (h->targetCapacity + 255) / 256;
+    if ((e = vm_launch_bin(h->dTargets.p, h->dPre.p + 6, 1, tb, 0, h->stream))) return cuda_fail(e, "target bin");
+    if ((e = vm_launch_scan(h->dTargets.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "target scan");
+    if ((e = vm_launch_scatter(h->dTargets.p, h->dPre.p + 6, 1, tb, nullptr, h->stream)))
+        return cuda_fail(e, "target scatter");
+    int live = 0;
+    if ((e = cudaMemcpyAsync(&live, h->start.p + h->cells, sizeof(int), cudaMemcpyDeviceToHost, h->stream)))
+        return cuda_fail(e, "live targets");
+    if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "target sort");
+    h->gridValid = false; // the grid buffers were borrowed
+    if (live != h->liveTargets) drop_graph(h);
+    h->liveTargets = live;
+    int qcap = std::max(live, 1); // every live target fits: the loss never overflows the queue
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    choose_loss_variant(h, sms);
+    int rc;
+    if ((rc = h->qitems.reserve(qcap))) return rc;
+    if ((e = vm_queue_init(h->queue.p, h->qitems.p, qcap, h->stream))) return cuda_fail(e, "queue");
+    return upload_tables(h);
+}
+
+} // namespace
+
+extern "C" {
+
+const char *vm_error_string(int code)
+{
+    switch (code) {
+    case VM_OK: return "ok";
+    case VM_ERR_ARG: return "invalid argument";
+    case VM_ERR_OOM: return "out of memory";
+    case VM_ERR_CUDA: return "CUDA error";
+    case VM_ERR_STATE: return "invalid state";
+    case VM_ERR_BUDGET: return "over memory budget";
+    case VM_ERR_TIMEOUT: return "timeout";
+    case VM_ERR_UNSUPPORTED: return "unsupported parameter";
+    case VM_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown error";
+    }
+}
+
+int vm_last_error(char *buf, int len)
+{
+    if (!buf || len <= 0) return VM_ERR_ARG;
+    std::snprintf(buf, (size_t)len, "%s", g_lastError.c_str());
+    return VM_OK;
+}
+
+int vm_version(int *major, int *minor, int *sm)
+{
+    if (major) *major = 1;
+    if (minor) *minor = 0;
+    if (sm) *sm = 103;
+    return VM_OK;
+}
+
+void vm_params_default(vm_params *p)
+{
+    if (!p) return;
+    p->iterations = 400;
+    p->localIterations = 100;
+    p->lrPerSpacing = 0.09f;
+    p->sampleFraction = 0.2f;
+    p->gamma = 0.5f;
+    p->milestones[0] = 80;
+    p->milestones[1] = 150;
+    p->milestones[2] = 200;
+    p->milestones[3] = 250;
+    p->seed = 1;
+    p->lossK = 12;
+}
+
+int vm_create(float width, float height, float spacing, const vm_params *params, vm_optimizer **out)
+{
+    if (!out) return fail(VM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!(width > 0.0f) || !(height > 0.0f) || !(spacing > 0.0f)) return fail(VM_ERR_ARG, "width, height and spacing must be > 0");
+    vm_params p;
+    vm_params_default(&p);
+    if (params) p = *params;
+    if (p.lossK != 8 && p.lossK != 12 && p.lossK != 16 && p.lossK != 24 && p.lossK != 32)
+        return fail(VM_ERR_UNSUPPORTED, "lossK must be 8, 12, 16, 24 or 32");
+    // hash grid: ceil(w / spacing) x ceil(h / spacing) (reference voro_optimizer.cu:520-521)
+    double gw = std::ceil(width / spacing), gh = std::ceil(height / spacing);
+    if (gw * gh > 1.5e9) return fail(VM_ERR_ARG, "hash grid too large");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return cuda_fail(e, "cudaGetDevice");
+    vm_optimizer *h = new vm_optimizer();
+    h->width = width;
+    h->height = height;
+    h->spacing = spacing;
+    h->params = p;
+    h->gridW = std::max(1, (int)std::ceil(width / spacing));
+    h->gridH = std::max(1, (int)std::ceil(height / spacing));
+    h->cells = h->gridW * h->gridH;
+    h->tiles = (h->cells + kScanTile - 1) / kScanTile;
+    int rc = VM_OK;
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) || (e = cudaEventCreate(&h->ev0)) ||
+        (e = cudaEventCreate(&h->ev1)))
+        rc = cuda_fail(e, "stream/event");
+    if (!rc) rc = h->counts.alloc(h->cells + 1);
+    if (!rc) rc = h->start.alloc(h->cells + 1);
+    if (!rc) rc = h->tileSums.alloc(h->tiles + 1);
+    if (!rc) rc = h->state.alloc(1);
+    if (!rc) rc = h->dFit.alloc(1);
+    if (!rc) rc = h->dSites.alloc(1);
+    if (!rc) rc = h->dTargets.alloc(1);
+    if (!rc) rc = h->dPre.alloc(8);
+    if (!rc) rc = h->flags.alloc(2);
+    if (!rc) rc = h->queue.alloc(vm_queue_bytes());
+    if (!rc && (e = vm_queue_init(h->queue.p, nullptr, 0, h->stream))) rc = cuda_fail(e, "queue");
+    if (!rc && (e = cudaMemset(h->counts.p, 0, sizeof(int) * (h->cells + 1)))) rc = cuda_fail(e, "memset");
+    if (!rc && (e = cudaMemset(h->state.p, 0, sizeof(VmState)))) rc = cuda_fail(e, "memset");
+    if (!rc) h->lossGrid = vm_loss_occupancy_blocks(h->lossVariant);
+    if (!rc) rc = upload_tables(h);
+    if (rc) {
+        vm_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return VM_OK;
+}
+
+int vm_destroy(vm_optimizer *h)
+{
+    if (!h) return VM_OK;
+    drop_graph(h);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h; // DevBuf members free their memory
+    return VM_OK;
+}
+
+int vm_set_targets(vm_optimizer *h, const float *xy, int n)
+{
+    if (!h || n < 0 || (n > 0 && !xy)) return fail(VM_ERR_ARG, "vm_set_targets: bad arguments");
+    int cap = std::max(n, 1);
+    int rc;
+    if (cap != h->targetCapacity) {
+        drop_graph(h);
+        h->targetCapacity = cap;
+        if ((rc = h->traw.alloc(cap)) || (rc = h->tkey.alloc(cap)) || (rc = h->trank.alloc(cap)) ||
+            (rc = h->tpos.alloc(cap)) || (rc = h->tslot.alloc(cap)))
+            return rc;
+    }
+    cudaError_t e;
+    // NaN padding fails every x >= 0 test (reference voro_optimizer.cu:558)
+    if ((e = cudaMemsetAsync(h->traw.p, 0xFF, sizeof(float2) * cap, h->stream))) return cuda_fail(e, "memset targets");
+    if (n > 0 && (e = cudaMemcpyAsync(h->traw.p, xy, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, h->stream)))
+        return cuda_fail(e, "upload targets");
+    if ((rc = upload_tables(h))) return rc;
+    return sort_targets(h);
+}
+
+int vm_update_targets(vm_optimizer *h, const int *dirty, int ndirty, const float *slots, int nslots)
+{
+    if (!h || ndirty < 0 || nslots < 0) return fail(VM_ERR_ARG, "vm_update_targets: bad arguments");
+    if (ndirty == 0) return VM_OK;
+    if (!dirty || !slots) return fail(VM_ERR_ARG, "vm_update_targets: NULL buffer");
+    if (nslots > h->targetCapacity) {
+        // grow with slack and re-upload everything (reference :566-571)
+        size_t cap = std::max((size_t)nslots * 3 / 2, (size_t)nslots + 64);
+        std::vector<float> padded(2 * cap, -1.0f);
+        std::memcpy(padded.data(), slots, sizeof(float) * 2 * (size_t)nslots);
+        return vm_set_targets(h, padded.data(), (int)cap);
+    }
+    std::vector<float2> values((size_t)ndirty);
+    for (int k = 0; k < ndirty; ++k) {
+        int s = dirty[k];
+        if (s < 0 || s >= nslots) return fail(VM_ERR_ARG, "vm_update_targets: dirty slot out of range");
+        values[k] = make_float2(slots[2 * (size_t)s], slots[2 * (size_t)s + 1]);
+    }
+    int rc;
+    if ((rc = h->stageSlots.reserve(ndirty)) || (rc = h->stageVals.reserve(ndirty))) return rc;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(h->stageSlots.p, dirty, sizeof(int) * ndirty, cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->stageVals.p, values.data(), sizeof(float2) * ndirty, cudaMemcpyHostToDevice,
+                             h->stream)) ||
+        (e = vm_launch_scatter_targets(h->traw.p, h->stageSlots.p, h->stageVals.p, ndirty, h->stream)))
+        return cuda_fail(e, "update targets");
+    return sort_targets(h);
+}
+
+int vm_set_occupancy(vm_optimizer *h, const uint64_t *masks, int tilesX, int tilesY, float voxelSize)
+{
+    if (!h || tilesX < 0 || tilesY < 0 || !(voxelSize > 0.0f)) return fail(VM_ERR_ARG, "vm_set_occupancy: bad arguments");
+    size_t n = (size_t)tilesX * tilesY;
+    if (n && !masks) return fail(VM_ERR_ARG, "vm_set_occupancy: NULL masks");
+    int rc;
+    if (tilesX != h->tilesX || tilesY != h->tilesY) {
+        h->tilesX = tilesX;
+        h->tilesY = tilesY;
+        if ((rc = h->occ.alloc(n))) return rc;
+    }
+    h->invVoxel = 1.0f / voxelSize;
+    cudaError_t e;
+    if (n && (e = cudaMemcpyAsync(h->occ.p, masks, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, h->stream)))
+        return cuda_fail(e, "upload occupancy");
+    if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "occupancy");
+    return VM_OK;
+}
+
+int vm_update_occupancy(vm_optimizer *h, const uint64_t *masks, int tx0, int ty0, int tx1, int ty1)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    tx0 = std::max(tx0, 0), ty0 = std::max(ty0, 0);
+    tx1 = std::min(tx1, h->tilesX), ty1 = std::min(ty1, h->tilesY);
+    if (tx0 >= tx1 || ty0 >= ty1) return VM_OK;
+    if (!masks) return fail(VM_ERR_ARG, "NULL masks");
+    size_t pitch = (size_t)h->tilesX * sizeof(uint64_t);
+    size_t off = (size_t)ty0 * h->tilesX + tx0;
+    cudaError_t e = cudaMemcpy2DAsync(h->occ.p + off, pitch, masks + off, pitch, (tx1 - tx0) * sizeof(uint64_t),
+                                      ty1 - ty0, cudaMemcpyHostToDevice, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cuda_fail(e, "update occupancy");
+    return VM_OK;
+}
+
+int vm_set_generators(vm_optimizer *h, const float *xy, int slotsW, int slotsH, float slotCellSize)
+{
+    if (!h || slotsW < 0 || slotsH < 0) return fail(VM_ERR_ARG, "vm_set_generators: bad arguments");
+    long long n64 = (long long)slotsW * slotsH;
+    if (n64 > 0x7FFFFFFF / kMaxCellVerts) return fail(VM_ERR_ARG, "too many generator slots");
+    int n = (int)n64;
+    if (n > 0 && !xy) return fail(VM_ERR_ARG, "vm_set_generators: NULL slots");
+    int rc;
+    if (slotsW != h->slotsW || slotsH != h->slotsH) {
+        drop_graph(h);
+        h->slotsW = slotsW;
+        h->slotsH = slotsH;
+        if ((rc = h->gen.alloc(n)) || (rc = h->m.alloc(n)) || (rc = h->v.alloc(n)) || (rc = h->gradX.alloc(2 * (size_t)n)) ||
+            (rc = h->key.alloc(n)) || (rc = h->rank.alloc(n)) || (rc = h->sortedIdx.alloc(n)) ||
+            (rc = h->sortedPos.alloc(n)))
+            return rc;
+        h->cellVerts.release();
+        h->cellEdges.release();
+        h->cellCount.release();
+        h->inside.release();
+    }
+    h->slotCellSize = slotCellSize;
+    cudaError_t e;
+    if (n > 0) {
+        if ((e = cudaMemcpyAsync(h->gen.p, xy, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, h->stream)) ||
+            (e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * 2 * (size_t)n, h->stream)))
+            return cuda_fail(e, "upload generators");
+    }
+    h->gridValid = false;
+    if ((rc = upload_tables(h))) return rc;
+    return vm_begin_schedule(h, h->params.iterations, 0, 0, h->slotsW, h->slotsH);
+}
+
+int vm_update_generators(vm_optimizer *h, const float *xy, int cx0, int cy0, int cx1, int cy1)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    cx0 = std::max(cx0, 0), cy0 = std::max(cy0, 0);
+    cx1 = std::min(cx1, h->slotsW), cy1 = std::min(cy1, h->slotsH);
+    if (cx0 >= cx1 || cy0 >= cy1) return VM_OK;
+    if (!xy) return fail(VM_ERR_ARG, "NULL slots");
+    size_t pitch = (size_t)h->slotsW * sizeof(float2);
+    size_t off = (size_t)cy0 * h->slotsW + cx0;
+    cudaError_t e = cudaMemcpy2DAsync(h->gen.p + off, pitch, reinterpret_cast<const float2 *>(xy) + off, pitch,
+                                      (cx1 - cx0) * sizeof(float2), cy1 - cy0, cudaMemcpyHostToDevice, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cuda_fail(e, "update generators");
+    h->gridValid = false;
+    return VM_OK;
+}
+
+int vm_begin_schedule(vm_optimizer *h, int iterations, int cx0, int cy0, int cx1, int cy1)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    cx0 = std::max(cx0, 0), cy0 = std::max(cy0, 0);
+    cx1 = std::min(cx1, h->slotsW), cy1 = std::min(cy1, h->slotsH);
+    VmFit &F = h->fit;
+    // RunParams (reference voro_optimizer.cu:658-675)
+    F.lr = h->params.lrPerSpacing * h->spacing;
+    F.gamma = h->params.gamma;
+    F.beta1 = 0.9f;
+    F.beta2 = 0.999f;
+    F.eps = 1e-8f;
+    for (int k = 0; k < 4; ++k)
+        F.milestones[k] = h->params.iterations != 0
+                              ? (int)std::lround(double(h->params.milestones[k]) * iterations / h->params.iterations)
+                              : h->params.milestones[k];
+    F.cx0 = cx0; F.cy0 = cy0; F.cx1 = cx1; F.cy1 = cy1;
+    float margin = 2.0f * h->spacing;
+    F.bx0 = (float)cx0 * h->slotCellSize - margin;
+    F.by0 = (float)cy0 * h->slotCellSize - margin;
+    F.bx1 = (float)cx1 * h->slotCellSize + margin;
+    F.by1 = (float)cy1 * h->slotCellSize + margin;
+    cudaError_t e;
+    if (cx0 < cx1 && cy0 < cy1) {
+        size_t pitch = (size_t)h->slotsW * sizeof(float2);
+        size_t off = (size_t)cy0 * h->slotsW + cx0;
+        if ((e = cudaMemset2DAsync(h->m.p + off, pitch, 0, (cx1 - cx0) * sizeof(float2), cy1 - cy0, h->stream)) ||
+            (e = cudaMemset2DAsync(h->v.p + off, pitch, 0, (cx1 - cx0) * sizeof(float2), cy1 - cy0, h->stream)))
+            return cuda_fail(e, "reset moments");
+    }
+    if ((e = cudaMemsetAsync(h->state.p, 0, sizeof(VmState), h->stream))) return cuda_fail(e, "reset state");
+    h->scheduleLength = iterations;
+    h->iteration = 0;
+    h->lastBatchLoss = 0.0f;
+    return upload_tables(h);
+}
+
+int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    if (gpuMs) *gpuMs = 0.0f;
+    if (iterations <= 0 || h->numSlots() == 0 || h->targetCapacity == 0) return VM_OK;
+    int rc;
+    if ((rc = ensure_grid(h))) return rc;
+    if ((rc = ensure_graph(h))) return rc;
+    cudaError_t e;
+    if ((e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "event");
+    for (int k = 0; k < iterations; ++k)
+        if ((e = cudaGraphLaunch(h->graph, h->stream))) return cuda_fail(e, "graph launch");
+    if ((e = cudaEventRecord(h->ev1, h->stream))) return cuda_fail(e, "event");
+    VmState st;
+    if ((rc = read_state(h, st))) return rc;
+    h->iteration = st.iter;
+    h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
+    h->exactTotal = st.slowTotal;
+    float ms = 0.0f;
+    if ((e = cudaEventElapsedTime(&ms, h->ev0, h->ev1))) return cuda_fail(e, "elapsed");
+    if (gpuMs) *gpuMs = ms;
+    return VM_OK;
+}
+
+int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
+{
+    if (!h || !stageMs || iterations < 0) return fail(VM_ERR_ARG, "bad arguments");
+    for (int k = 0; k < 4; ++k) stageMs[k] = 0.0f;
+    if (iterations == 0 || h->numSlots() == 0 || h->targetCapacity == 0) return VM_OK;
+    int rc;
+    if ((rc = ensure_grid(h))) return rc;
+    size_t need = (size_t)iterations * 5;
+    cudaError_t e;
+    while (h->timing.size() < need) {
+        cudaEvent_t ev;
+        if ((e = cudaEventCreate(&ev))) return cuda_fail(e, "event");
+        h->timing.push_back(ev);
+    }
+    int n = h->numSlots();
+    int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
+    for (int k = 0; k < iterations; ++k) {
+        cudaEvent_t *ev = &h->timing[(size_t)k * 5];
+        if ((e = cudaEventRecord(ev[0], h->stream)) ||
+            (e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+            (e = cudaEventRecord(ev[1], h->stream)) ||
+            (e = vm_launch_adam_bin(h->dFit.p, h->dPre.p + 0, 1, (n + 255) / 256, h->queue.p, h->stream)) ||
+            (e = cudaEventRecord(ev[2], h->stream)) ||
+            (e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream)) ||
+            (e = cudaEventRecord(ev[3], h->stream)) ||
+            (e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, h->dFit.p, h->stream)) ||
+            (e = cudaEventRecord(ev[4], h->stream)))
+            return cuda_fail(e, "timed step");
+    }
+    VmState st;
+    if ((rc = read_state(h, st))) return rc;
+    h->iteration = st.iter;
+    h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
+    h->exactTotal = st.slowTotal;
+    for (int k = 0; k < iterations; ++k) {
+        cudaEvent_t *ev = &h->timing[(size_t)k * 5];
+        for (int j = 0; j < 4; ++j) {
+            float ms = 0.0f;
+            if ((e = cudaEventElapsedTime(&ms, ev[j], ev[j + 1]))) return cuda_fail(e, "elapsed");
+            stageMs[j] += ms / iterations;
+        }
+    }
+    return VM_OK;
+}
+
+int vm_set_loss_variant(vm_optimizer *h, int variant)
+{
+    if (!h || variant < -1 || variant >= vm_loss_variants()) return fail(VM_ERR_ARG, "bad loss variant");
+    h->lossForced = variant;
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    choose_loss_variant(h, sms);
+    drop_graph(h);
+    return upload_tables(h);
+}
+
+int vm_get_loss_variant(vm_optimizer *h, int *variant, int *count)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    if (variant) *variant = h->lossVariant;
+    if (count) *count = vm_loss_variants();
+    return VM_OK;
+}
+
+int vm_evaluate_loss(vm_optimizer *h, float *loss)
+{
+    if (!h || !loss) return fail(VM_ERR_ARG, "bad arguments");
+    *loss = 0.0f;
+    if (h->numSlots() == 0 || h->targetCapacity == 0) return VM_OK;
+    int rc;
+    if ((rc = ensure_grid(h))) return rc;
+    cudaError_t e;
+    int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 1, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+        (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream)))
+        return cuda_fail(e, "evaluate loss");
+    VmState st;
+    if ((rc = read_state(h, st))) return rc;
+    *loss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
+    return VM_OK;
+}
+
+int vm_info(vm_optimizer *h, vm_info_t *out)
+{
+    if (!h || !out) return fail(VM_ERR_ARG, "bad arguments");
+    out->iteration = h->iteration;
+    out->scheduleLength = h->scheduleLength;
+    out->numSlots = h->numSlots();
+    out->targetCapacity = h->targetCapacity;
+    out->liveTargets = h->liveTargets;
+    out->gridW = h->gridW;
+    out->gridH = h->gridH;
+    out->lastBatchLoss = h->lastBatchLoss;
+    out->exactTargets = h->exactTotal;
+    return VM_OK;
+}
+
+int vm_get_generators(vm_optimizer *h, float *xy)
+{
+    if (!h || !xy) return fail(VM_ERR_ARG, "bad arguments");
+    int n = h->numSlots();
+    if (!n) return VM_OK;
+    cudaError_t e = cudaMemcpyAsync(xy, h->gen.p, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToHost, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cuda_fail(e, "read generators");
+    return VM_OK;
+}
+
+int vm_get_moments(vm_optimizer *h, float *m, float *v)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    int n = h->numSlots();
+    cudaError_t e = cudaSuccess;
+    if (n && m) e = cudaMemcpyAsync(m, h->m.p, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToHost, h->stream);
+    if (!e && n && v) e = cudaMemcpyAsync(v, h->v.p, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToHost, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cuda_fail(e, "read moments");
+    return VM_OK;
+}
+
+int vm_get_grid(vm_optimizer *h, int *start, int *sortedIdx, float *sortedPos, int *genCell)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    int rc;
+    if (h->numSlots() == 0) return VM_OK;
+    if ((rc = ensure_grid(h))) return rc;
+    int live = 0;
+    cudaError_t e = cudaMemcpyAsync(&live, h->start.p + h->cells, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (!e && start) e = cudaMemcpyAsync(start, h->start.p, sizeof(int) * (size_t)(h->cells + 1), cudaMemcpyDeviceToHost, h->stream);
+    if (!e && sortedIdx) e = cudaMemcpyAsync(sortedIdx, h->sortedIdx.p, sizeof(int) * (size_t)live, cudaMemcpyDeviceToHost, h->stream);
+    if (!e && sortedPos) e = cudaMemcpyAsync(sortedPos, h->sortedPos.p, sizeof(float2) * (size_t)live, cudaMemcpyDeviceToHost, h->stream);
+    if (!e && genCell) e = cudaMemcpyAsync(genCell, h->key.p, sizeof(int) * (size_t)h->numSlots(), cudaMemcpyDeviceToHost, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cuda_fail(e, "read grid");
+    return VM_OK;
+}
+
+int vm_knn(vm_optimizer *h, const float *queries, int nq, int K, int *idx, float *d2)
+{
+    if (!h || nq < 0 || (nq > 0 && (!queries || !idx || !d2))) return fail(VM_ERR_ARG, "vm_knn: bad arguments");
+    if (K != 8 && K != 12 && K != 16 && K != 24 && K != 32) return fail(VM_ERR_UNSUPPORTED, "K must be 8, 12, 16, 24 or 32");
+    if (nq == 0) return VM_OK;
+    if (h->numSlots() == 0) return fail(VM_ERR_STATE, "no generators");
+    int rc;
+    if ((rc = ensure_grid(h))) return rc;
+    if ((rc = h->qbuf.reserve(nq)) || (rc = h->kIdx.reserve((size_t)nq * K)) || (rc = h->kD2.reserve((size_t)nq * K)))
+        return rc;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(h->qbuf.p, queries, sizeof(float2) * (size_t)nq, cudaMemcpyHostToDevice, h->stream)) ||
+        (e = vm_launch_knn(h->dFit.p, h->qbuf.p, nq, K, h->kIdx.p, h->kD2.p, h->stream)) ||
+        (e = cudaMemcpyAsync(idx, h->kIdx.p, sizeof(int) * (size_t)nq * K, cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(d2, h->kD2.p, sizeof(float) * (size_t)nq * K, cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaStreamSynchronize(h->stream)))
+        return cuda_fail(e, "knn");
+    return VM_OK;
+}
+
+int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *grad, int *count, float *lossSum)
+{
+    if (!h || (mode != 0 && mode != 1)) return fail(VM_ERR_ARG, "vm_probe: bad arguments");
+    int n = h->numSlots();
+    if (n == 0 || h->targetCapacity == 0) return fail(VM_ERR_STATE, "no generators or targets");
+    int rc;
+    if ((rc = ensure_grid(h))) return rc;
+    int live = h->liveTargets;
+    if ((rc = h->dbgI0.reserve(std::max(live, 1))) || (rc = h->dbgJ.reserve(std::max(live, 1))) ||
+        (rc = h->dbgLoss.reserve(std::max(live, 1))))
+        return rc;
+    VmFit saved = h->fit;
+    h->fit.dbgI0 = h->dbgI0.p;
+    h->fit.dbgJ = h->dbgJ.p;
+    h->fit.dbgLoss = h->dbgLoss.p;
+    if ((rc = upload_tables(h))) return rc;
+    cudaError_t e;
+    int lossTiles = (live + h->lossTile - 1) / h->lossTile;
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, mode, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+        (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream))) {
+        h->fit = saved;
+        upload_tables(h);
+        return cuda_fail(e, "probe");
+    }
+    std::vector<int> hi0(live), hj(live), slot(live);
+    std::vector<float> hl(live);
+    std::vector<long long> g(grad ? 2 * (size_t)n : 0);
+    VmState st;
+    if (live > 0) {
+        if ((e = cudaMemcpyAsync(hi0.data(), h->dbgI0.p, sizeof(int) * live, cudaMemcpyDeviceToHost, h->stream)) ||
+            (e = cudaMemcpyAsync(hj.data(), h->dbgJ.p, sizeof(int) * live, cudaMemcpyDeviceToHost, h->stream)) ||
+            (e = cudaMemcpyAsync(hl.data(), h->dbgLoss.p, sizeof(float) * live, cudaMemcpyDeviceToHost, h->stream)) ||
+            (e = cudaMemcpyAsync(slot.data(), h->tslot.p, sizeof(int) * live, cudaMemcpyDeviceToHost, h->stream)))
+            return cuda_fail(e, "probe read");
+    }
+    if (grad && (e = cudaMemcpyAsync(g.data(), h->gradX.p, sizeof(long long) * 2 * n, cudaMemcpyDeviceToHost, h->stream)))
+        return cuda_fail(e, "probe grad");
+    if ((e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * 2 * (size_t)n, h->stream))) return cuda_fail(e, "probe clear");
+    if ((rc = read_state(h, st))) return rc;
+    h->fit = saved;
+    if ((rc = upload_tables(h))) return rc;
+    int cap = h->targetCapacity;
+    if (i0) std::fill(i0, i0 + cap, -1);
+    if (j) std::fill(j, j + cap, -1);
+    if (loss) std::fill(loss, loss + cap, 0.0f);
+    for (int t = 0; t < live; ++t) {
+        int s = slot[t];
+        if (s < 0 || s >= cap) continue;
+        if (i0) i0[s] = hi0[t];
+        if (j) j[s] = hj[t];
+        if (loss) loss[s] = hl[t];
+    }
+    if (grad) {
+        float scale = std::ldexp(1.0f, -h->fit.gradExp);
+        for (size_t k = 0; k < 2 * (size_t)n; ++k) grad[k] = (float)g[k] * scale;
+    }
+    if (count) *count = st.count;
+    if (lossSum) *lossSum = st.loss;
+    return VM_OK;
+}
+
+int vm_extract(vm_optimizer *h, vm_mesh_info *info)
+{
+    if (!h || !info) return fail(VM_ERR_ARG, "bad arguments");
+    std::memset(info, 0, sizeof(*info));
+    h->mesh = MeshHost();
+    int n = h->numSlots();
+    if (n == 0) return VM_OK;
+    int rc;
+    if ((rc = h->cellVerts.reserve((size_t)n * kMaxCellVerts)) || (rc = h->cellEdges.reserve((size_t)n * kMaxCellVerts)) ||
+        (rc = h->cellCount.reserve(n)) || (rc = h->inside.reserve(n)))
+        return rc;
+    cudaError_t e;
+    if ((e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "event");
+    if ((rc = ensure_grid(h))) return rc;
+    if ((e = cudaMemsetAsync(h->flags.p, 0, 2 * sizeof(int), h->stream)) ||
+        (e = vm_launch_cells_n(h->dFit.p, n, h->occ.p, h->tilesX, h->tilesY, h->invVoxel, h->cellVerts.p,
+                               h->cellEdges.p, h->cellCount.p, h->inside.p, h->flags.p, h->stream)) ||
+        (e = cudaEventRecord(h->ev1, h->stream)) || (e = cudaEventSynchronize(h->ev1)))
+        return cuda_fail(e, "extract");
+    cudaEventElapsedTime(&h->mesh.gpuMs, h->ev0, h->ev1);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<float2> verts((size_t)n * kMaxCellVerts);
+    std::vector<int> labels((size_t)n * kMaxCellVerts), counts(n);
+    int flags[2];
+    MeshHost &M = h->mesh;
+    M.generators.resize(n);
+    M.inside.resize(n);
+    if ((e = cudaMemcpyAsync(verts.data(), h->cellVerts.p, sizeof(float2) * verts.size(), cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(labels.data(), h->cellEdges.p, sizeof(int) * labels.size(), cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(counts.data(), h->cellCount.p, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(M.inside.data(), h->inside.p, n, cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(M.generators.data(), h->gen.p, sizeof(float2) * n, cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(flags, h->flags.p, sizeof(flags), cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaStreamSynchronize(h->stream)))
+        return cuda_fail(e, "extract read");
+    M.unsafeCells = flags[0];
+    M.overflowCells = flags[1];
+    assemble_boundary(verts, labels, counts, M.inside, n, M);
+    M.hostMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    info->numGenerators = n;
+    info->numCellVerts = (int)M.cellVerts.size();
+    info->numVertices = (int)M.vertices.size();
+    info->numEdges = (int)(M.edges.size() / 2);
+    info->watertight = M.watertight ? 1 : 0;
+    info->loops = M.loops;
+    info->unsafeCells = M.unsafeCells;
+    info->overflowCells = M.overflowCells;
+    info->gpuMs = M.gpuMs;
+    info->hostMs = M.hostMs;
+    return VM_OK;
+}
+
+int vm_mesh_copy(vm_optimizer *h, float *generators, uint8_t *inside, int *cellStart, float *cellVerts, float *vertices,
+                 int *edges, int *cellLabels)
+{
+    if (!h) return fail(VM_ERR_ARG, "NULL handle");
+    const MeshHost &M = h->mesh;
+    if (generators) std::memcpy(generators, M.generators.data(), sizeof(float2) * M.generators.size());
+    if (inside) std::memcpy(inside, M.inside.data(), M.inside.size());
+    if (cellStart) std::memcpy(cellStart, M.cellStart.data(), sizeof(int) * M.cellStart.size());
+    if (cellVerts) std::memcpy(cellVerts, M.cellVerts.data(), sizeof(float2) * M.cellVerts.size());
+    if (vertices) std::memcpy(vertices, M.vertices.data(), sizeof(float2) * M.vertices.size());
+    if (edges) std::memcpy(edges, M.edges.data(), sizeof(int) * M.edges.size());
+    if (cellLabels) std::memcpy(cellLabels, M.cellLabels.data(), sizeof(int) * M.cellLabels.size());
+    return VM_OK;
+}
+
+// ===========================================================================
+// Poisson sampler
+// ===========================================================================
+} // extern "C"
+
+struct pd_sampler {
+    float width, height, radius, cellSize;
+    int gridW, gridH, trials;
+    unsigned seed, roundBase = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    DevBuf<float2> grid;
+    std::vector<float2> cells;
+};
+
+extern "C" {
+
+int pd_create(float width, float height, float radius, int trials, unsigned seed, pd_sampler **out)
+{
+    if (!out) return fail(VM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!(width > 0.0f) || !(height > 0.0f) || !(radius > 0.0f) || trials < 0)
+        return fail(VM_ERR_ARG, "width, height, radius must be > 0 and trials >= 0");
+    pd_sampler *s = new pd_sampler();
+    s->width = width;
+    s->height = height;
+    s->radius = radius;
+    // Sampler::Sampler (reference poisson_disk.cu:120-125)
+    s->cellSize = radius / sqrtf(2.0f);
+    double gw = std::ceil((double)(width / s->cellSize)), gh = std::ceil((double)(height / s->cellSize));
+    if (gw * gh > 2.0e9) {
+        delete s;
+        return fail(VM_ERR_ARG, "sampler grid too large");
+    }
+    s->gridW = (int)ceilf(width / s->cellSize);
+    s->gridH = (int)ceilf(height / s->cellSize);
+    s->trials = trials;
+    s->seed = seed;
+    size_t nCells = (size_t)s->gridW * s->gridH;
+    s->cells.assign(nCells, make_float2(-1.0f, -1.0f));
+    cudaError_t e;
+    int rc = VM_OK;
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) || (e = cudaEventCreate(&s->ev0)) ||
+        (e = cudaEventCreate(&s->ev1)))
+        rc = cuda_fail(e, "sampler stream");
+    if (!rc) rc = s->grid.alloc(nCells);
+    if (!rc) rc = pd_resample(s, 0, 0, s->gridW, s->gridH, nullptr);
+    if (rc) {
+        pd_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return VM_OK;
+}
+
+int pd_destroy(pd_sampler *s)
+{
+    if (!s) return VM_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return VM_OK;
+}
+
+int pd_resample(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, float *gpuMs)
+{
+    if (!s) return fail(VM_ERR_ARG, "NULL sampler");
+    if (gpuMs) *gpuMs = 0.0f;
+    int x0 = std::max(cx0, 0), y0 = std::max(cy0, 0), x1 = std::min(cx1, s->gridW), y1 = std::min(cy1, s->gridH);
+    if (x0 >= x1 || y0 >= y1) return VM_OK;
+    PdParams p{s->width, s->height, s->radius, s->cellSize, s->gridW, s->gridH, s->seed};
+    cudaError_t e;
+    if ((e = cudaEventRecord(s->ev0, s->stream)) ||
+        (e = pd_launch_resample(s->grid.p, p, x0, y0, x1, y1, s->trials, s->roundBase, s->stream)) ||
+        (e = cudaEventRecord(s->ev1, s->stream)))
+        return cuda_fail(e, "resample");
+    s->roundBase += (unsigned)s->trials;
+    size_t pitch = (size_t)s->gridW * sizeof(float2);
+    size_t off = (size_t)y0 * s->gridW + x0;
+    if ((e = cudaMemcpy2DAsync(s->cells.data() + off, pitch, s->grid.p + off, pitch, (x1 - x0) * sizeof(float2), y1 - y0,
+                               cudaMemcpyDeviceToHost, s->stream)) ||
+        (e = cudaStreamSynchronize(s->stream)))
+        return cuda_fail(e, "resample read");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    if (gpuMs) *gpuMs = ms;
+    return VM_OK;
+}
+
+int pd_info(pd_sampler *s, pd_info_t *out)
+{
+    if (!s || !out) return fail(VM_ERR_ARG, "bad arguments");
+    out->width = s->width;
+    out->height = s->height;
+    out->radius = s->radius;
+    out->cellSize = s->cellSize;
+    out->gridW = s->gridW;
+    out->gridH = s->gridH;
+    out->trials = s->trials;
+    out->seed = s->seed;
+    out->roundBase = s->roundBase;
+    return VM_OK;
+}
+
+int pd_cells(pd_sampler *s, float *xy)
+{
+    if (!s || !xy) return fail(VM_ERR_ARG, "bad arguments");
+    std::memcpy(xy, s->cells.data(), sizeof(float2) * s->cells.size());
+    return VM_OK;
+}
+
+// Sampler::Verify (reference poisson_disk.cu:179-199)
+int pd_verify(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, int *ok)
+{
+    if (!s || !ok) return fail(VM_ERR_ARG, "bad arguments");
+    float r2 = s->radius * s->radius;
+    int W = s->gridW, H = s->gridH;
+    int vx0 = std::max(cx0 - 2, 0), vx1 = std::min(cx1 + 2, W);
+    int vy0 = std::max(cy0 - 2, 0), vy1 = std::min(cy1 + 2, H);
+    *ok = 1;
+    for (int cy = vy0; cy < vy1; ++cy)
+        for (int cx = vx0; cx < vx1; ++cx) {
+            float2 a = s->cells[(size_t)cy * W + cx];
+            if (a.x < 0) continue;
+            for (int ny = std::max(cy - 2, 0); ny <= std::min(cy + 2, H - 1); ++ny)
+                for (int nx = std::max(cx - 2, 0); nx <= std::min(cx + 2, W - 1); ++nx) {
+                    if (nx == cx && ny == cy) continue;
+                    float2 b = s->cells[(size_t)ny * W + nx];
+                    if (b.x < 0) continue;
+                    float dx = a.x - b.x, dy = a.y - b.y;
+                    if (dx * dx + dy * dy < r2) {
+                        *ok = 0;
+                        return VM_OK;
+                    }
+                }
+        }
+    return VM_OK;
+}
+
+int pd_count(pd_sampler *s, long long *n)
+{
+    if (!s || !n) return fail(VM_ERR_ARG, "bad arguments");
+    long long c = 0;
+    for (const float2 &p : s->cells) c += p.x >= 0.0f;
+    *n = c;
+    return VM_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,175 @@
+/*
+ * vm_capi.h — C ABI of libvoromesh_gb300.so: the GB300 VoroMesh optimiser,
+ * Voronoi extraction and Poisson-disk sampler.
+ *
+ * The reference exposes this path as two C++ classes
+ * (voromesh::VoroOptimizer, include/voromesh/voro_optimizer.h:70-138, and
+ * poisson::Sampler, include/poisson/poisson_disk.h:21-62). Each vm_* / pd_*
+ * entry point below is one of their methods, flattened to plain pointers and
+ * sizes: float pairs are (x, y) interleaved like Vec2 / Sample / float2, and
+ * every host buffer is copied before the call returns, as the reference's
+ * synchronous cudaMemcpy calls do. The library also implements the two C++
+ * classes on top of these functions (include/voromesh, include/poisson).
+ *
+ * Every function returns VM_OK (0) or one of the VM_ERR_* codes; the message
+ * of the last failure on the calling thread is available from
+ * vm_last_error(). The C++ classes turn a non-zero status into the
+ * reference's behaviour (message on stderr, exit(1)).
+ *
+ * Threading follows the reference: one handle is not thread-safe; separate
+ * handles are independent. Each optimiser owns a non-blocking CUDA stream.
+ */
+#ifndef VM_CAPI_H
+#define VM_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    VM_OK = 0,
+    VM_ERR_ARG = 1,         /* invalid argument or size */
+    VM_ERR_OOM = 2,         /* device or host allocation failed */
+    VM_ERR_CUDA = 3,        /* CUDA runtime or kernel error */
+    VM_ERR_STATE = 4,       /* call not valid in the current state */
+    VM_ERR_BUDGET = 5,      /* request exceeds the memory budget (batch / serving) */
+    VM_ERR_TIMEOUT = 6,     /* a bounded wait gave up */
+    VM_ERR_UNSUPPORTED = 7, /* parameter outside what the kernels implement */
+    VM_ERR_NODEVICE = 8     /* no CUDA device */
+};
+
+const char *vm_error_string(int code);
+/* Copies the last failure message of this thread into buf (NUL-terminated). */
+int vm_last_error(char *buf, int len);
+/* Library version and the compute capability it was built for (e.g. 103). */
+int vm_version(int *major, int *minor, int *sm);
+
+/* ---- VoroMesh optimiser (voromesh::VoroOptimizer) ---------------------------- */
+
+/* OptimizerParams (include/voromesh/voro_optimizer.h:34-44) plus the kNN size
+ * of the loss, a compile-time constant (kLossK = 12) in the reference
+ * (src/voromesh/voro_optimizer.cu:54). Supported lossK: 8, 12, 16, 24, 32. */
+typedef struct {
+    int iterations;      /* 400 */
+    int localIterations; /* 100 */
+    float lrPerSpacing;  /* 0.09 */
+    float sampleFraction;/* 0.2 */
+    float gamma;         /* 0.5 */
+    int milestones[4];   /* 80 150 200 250 */
+    unsigned seed;       /* 1 */
+    int lossK;           /* 12 */
+} vm_params;
+
+typedef struct vm_optimizer vm_optimizer;
+
+typedef struct {
+    int iteration;        /* Iteration() */
+    int scheduleLength;   /* ScheduleLength() */
+    int numSlots;         /* NumSlots() */
+    int targetCapacity;   /* target slots allocated */
+    int liveTargets;      /* targets with x >= 0 */
+    int gridW, gridH;     /* hash grid */
+    float lastBatchLoss;  /* LastBatchLoss() */
+    long long exactTargets; /* targets resolved by the exact ring search so far */
+} vm_info_t;
+
+typedef struct {
+    int numGenerators;  /* slots */
+    int numCellVerts;   /* CSR vertices of all cells */
+    int numVertices;    /* boundary vertices */
+    int numEdges;       /* boundary edges */
+    int watertight, loops, unsafeCells, overflowCells;
+    float gpuMs, hostMs;
+} vm_mesh_info;
+
+/* OptimizerParams{} defaults */
+void vm_params_default(vm_params *p);
+/* VoroOptimizer(width, height, spacing, params)  voro_optimizer.h:75 */
+int vm_create(float width, float height, float spacing, const vm_params *params, vm_optimizer **out);
+/* ~VoroOptimizer()  voro_optimizer.h:76 */
+int vm_destroy(vm_optimizer *h);
+/* SetTargets(slots)  voro_optimizer.h:82; xy holds n (x,y) pairs */
+int vm_set_targets(vm_optimizer *h, const float *xy, int n);
+/* UpdateTargets(dirty, slots)  voro_optimizer.h:84 */
+int vm_update_targets(vm_optimizer *h, const int *dirty, int ndirty, const float *slots, int nslots);
+/* SetOccupancy(masks, tilesX, tilesY, voxelSize)  voro_optimizer.h:87 */
+int vm_set_occupancy(vm_optimizer *h, const uint64_t *masks, int tilesX, int tilesY, float voxelSize);
+/* UpdateOccupancy(masks, tx0, ty0, tx1, ty1)  voro_optimizer.h:89 */
+int vm_update_occupancy(vm_optimizer *h, const uint64_t *masks, int tx0, int ty0, int tx1, int ty1);
+/* SetGenerators(slots, slotsW, slotsH, slotCellSize)  voro_optimizer.h:94 */
+int vm_set_generators(vm_optimizer *h, const float *xy, int slotsW, int slotsH, float slotCellSize);
+/* UpdateGenerators(slots, cx0, cy0, cx1, cy1)  voro_optimizer.h:96 */
+int vm_update_generators(vm_optimizer *h, const float *xy, int cx0, int cy0, int cx1, int cy1);
+/* BeginSchedule(iterations, cx0, cy0, cx1, cy1)  voro_optimizer.h:102 */
+int vm_begin_schedule(vm_optimizer *h, int iterations, int cx0, int cy0, int cx1, int cy1);
+/* Step(iterations) -> GPU ms  voro_optimizer.h:106 */
+int vm_step(vm_optimizer *h, int iterations, float *gpuMs);
+/* Step(iterations) run kernel by kernel with CUDA events between the stages;
+ * stageMs[4] receives the mean ms per step of: loss (fast path + exact
+ * queue), Adam + binning, cell-count scan, cell-sorted scatter. An addition
+ * (no counterpart in the reference) used to attribute step time. */
+int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs);
+/* Loss-kernel variant (block size, occupancy target, gradient aggregation):
+ * -1 = automatic. All variants produce identical results; the autotuner
+ * picks the fastest per fit-size bucket. Additions, no reference counterpart. */
+int vm_set_loss_variant(vm_optimizer *h, int variant);
+int vm_get_loss_variant(vm_optimizer *h, int *variant, int *count);
+/* EvaluateLoss()  voro_optimizer.h:113 */
+int vm_evaluate_loss(vm_optimizer *h, float *loss);
+/* Iteration / ScheduleLength / NumSlots / LastBatchLoss  voro_optimizer.h:111,118-120 */
+int vm_info(vm_optimizer *h, vm_info_t *out);
+/* Current generator slots (numSlots pairs). */
+int vm_get_generators(vm_optimizer *h, float *xy);
+/* Adam moments (numSlots pairs each; either may be NULL). */
+int vm_get_moments(vm_optimizer *h, float *m, float *v);
+/* Extract()  voro_optimizer.h:116: runs the clipper and boundary assembly and
+ * keeps the result in the handle; sizes in *info, arrays via vm_mesh_copy. */
+int vm_extract(vm_optimizer *h, vm_mesh_info *info);
+/* Copies the last Extract(): generators (2n), inside (n), cellStart (n+1),
+ * cellVerts (2 numCellVerts), vertices (2 numVertices), edges (2 numEdges);
+ * cellLabels (numCellVerts edge labels) is an addition. Any may be NULL. */
+int vm_mesh_copy(vm_optimizer *h, float *generators, uint8_t *inside, int *cellStart, float *cellVerts,
+                 float *vertices, int *edges, int *cellLabels);
+
+/* ---- inspection (used by the parity tests) ----------------------------------- */
+/* The hash grid of the current generators: start (gridW*gridH+1), sortedIdx and
+ * sortedPos (live sites, cell order, ascending slot within a cell), genCell (numSlots). */
+int vm_get_grid(vm_optimizer *h, int *start, int *sortedIdx, float *sortedPos, int *genCell);
+/* Exact K nearest generators (K in 8,12,16,24,32) of nq query points, (d2, index) order. */
+int vm_knn(vm_optimizer *h, const float *queries, int nq, int K, int *idx, float *d2);
+/* One loss pass without moving anything. mode 0: the next Step's pass (active
+ * box, subsample, gradient); mode 1: EvaluateLoss's pass. Per target slot
+ * (targetCapacity entries, any may be NULL): nearest site, bisector
+ * neighbour, loss (-1/-1/0 when unused). grad: 2*numSlots summed gradient
+ * (mode 0). count, lossSum: the pass totals. */
+int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *grad, int *count, float *lossSum);
+
+/* ---- Poisson-disk sampler (poisson::Sampler) ---------------------------------- */
+typedef struct pd_sampler pd_sampler;
+typedef struct {
+    float width, height, radius, cellSize;
+    int gridW, gridH, trials;
+    unsigned seed, roundBase;
+} pd_info_t;
+
+/* Sampler(width, height, radius, trials, seed): fills the whole domain  poisson_disk.h:24 */
+int pd_create(float width, float height, float radius, int trials, unsigned seed, pd_sampler **out);
+int pd_destroy(pd_sampler *s);
+/* Resample(cx0, cy0, cx1, cy1) -> GPU ms  poisson_disk.h:33 */
+int pd_resample(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, float *gpuMs);
+/* Width/Height/Radius/CellSize/GridW/GridH/Trials  poisson_disk.h:44-50 */
+int pd_info(pd_sampler *s, pd_info_t *out);
+/* Cells(): gridW*gridH (x,y) pairs, x < 0 = empty  poisson_disk.h:41 */
+int pd_cells(pd_sampler *s, float *xy);
+/* Verify(cx0, cy0, cx1, cy1)  poisson_disk.h:37 */
+int pd_verify(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, int *ok);
+/* Number of samples in the grid. */
+int pd_count(pd_sampler *s, long long *n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,107 @@
+"""GPU fit parity: the CUDA optimiser against the CPU oracle, bit-exact.
+
+The product sums gradients and losses in order-independent fixed point, so
+its trajectory is a deterministic function of the inputs and the oracle
+(same arithmetic, same sums) must reproduce it exactly, step for step.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(vm, orc, gen, tgt, spacing, K, steps, fraction, slots=None, seed=1, iters=300, lr_ps=0.09):
+    from voromesh_gb300 import OptimizerParams, VoroOptimizer
+
+    sw, sh = slots or (len(gen), 1)
+    p = OptimizerParams(iterations=iters, sampleFraction=fraction, lrPerSpacing=lr_ps, lossK=K, seed=seed)
+    opt = VoroOptimizer(2.0, 2.0, spacing, p)
+    opt.SetTargets(tgt)
+    opt.SetGenerators(gen, sw, sh, 2.0)
+    ref = orc.Fit(2.0, 2.0, spacing, K, lr_ps, fraction, iters, seed=seed)
+    ref.set_targets(tgt)
+    ref.set_generators(gen, sw, sh, 2.0)
+    return opt, ref
+
+
+@pytest.mark.parametrize("K,fraction", [(12, 1.0), (12, 0.2), (16, 1.0), (8, 0.5), (32, 1.0)])
+def test_fit_bit_exact(vm, orc, K, fraction):
+    from voromesh_gb300 import synth
+
+    gen = synth.uniform(3, 1, 1024)
+    tgt = synth.circle(3, 2, 8192, 0.6, 1e-3)
+    opt, ref = _pair(vm, orc, gen, tgt, 0.06, K, 0, fraction)
+    for chunk in (1, 4, 15):
+        opt.Step(chunk)
+        lref = ref.step(chunk)
+        g, m, v = ref.generators()
+        assert np.array_equal(opt.Generators(), g)
+        om, ov = opt.Moments()
+        assert np.array_equal(om, m) and np.array_equal(ov, v)
+        assert np.float32(opt.LastBatchLoss()) == np.float32(lref)
+    assert opt.Iteration() == ref.iteration() == 20
+    assert np.float32(opt.EvaluateLoss()) == np.float32(ref.eval_loss())
+
+
+def test_exact_path_targets(vm, orc):
+    """Targets far from every generator (outside the domain, in empty regions)
+    miss the block certificates and take the deferred exact ring search."""
+    from voromesh_gb300 import synth
+
+    gen = synth.uniform(4, 1, 600, -0.5, 0.5)  # generators in the middle only
+    tgt = np.concatenate([synth.circle(4, 2, 3000, 0.9, 0.05), synth.uniform(4, 3, 500, -1.2, 1.2)])
+    opt, ref = _pair(vm, orc, gen, tgt, 0.05, 16, 0, 1.0)
+    opt.Step(6)
+    lref = ref.step(6)
+    assert opt.info().exactTargets > 0
+    assert np.array_equal(opt.Generators(), ref.generators()[0])
+    assert np.float32(opt.LastBatchLoss()) == np.float32(lref)
+    i0, j, loss, _, cnt, _ = opt.Probe(1)
+    ri0, rj, rloss = orc.loss_detail(ref, tgt, 16)
+    assert np.array_equal(i0, ri0) and np.array_equal(j, rj) and np.array_equal(loss, rloss)
+
+
+def test_grid_bit_exact(vm, orc):
+    from voromesh_gb300 import synth
+
+    gen = synth.uniform(5, 1, 3000)
+    gen[::7] = -1.0  # empty slots
+    tgt = synth.circle(5, 2, 4000, 0.5, 1e-2)
+    opt, ref = _pair(vm, orc, gen, tgt, 0.05, 12, 0, 1.0)
+    start, sidx, spos, gcell = opt.Grid()
+    r = ref.grid()
+    assert np.array_equal(start, r[0]) and np.array_equal(sidx, r[1])
+    assert np.array_equal(spos, r[2]) and np.array_equal(gcell, r[3])
+    opt.Step(3)
+    ref.step(3)
+    start, sidx, spos, gcell = opt.Grid()
+    r = ref.grid()
+    assert np.array_equal(start, r[0]) and np.array_equal(sidx, r[1]) and np.array_equal(gcell, r[3])
+
+
+@pytest.mark.parametrize("K", [8, 12, 16, 24, 32])
+def test_knn_bit_exact(vm, orc, K):
+    from voromesh_gb300 import synth
+
+    gen = synth.uniform(9, 1, 2000)
+    q = synth.uniform(9, 2, 3000)
+    opt, _ = _pair(vm, orc, gen, q, 0.05, 12, 0, 1.0)
+    idx, d2 = opt.Knn(q, K)
+    grid = orc.Grid(gen, 40, 40, 0.05)
+    ridx, rd2 = grid.knn(q, K)
+    assert np.array_equal(idx, ridx)
+    assert np.array_equal(d2, rd2)
+
+
+def test_probe_matches_oracle(vm, orc):
+    """Per-target decisions (nearest site, bisector neighbour, loss) and the summed gradient."""
+    from voromesh_gb300 import synth
+
+    gen = synth.uniform(11, 1, 800)
+    tgt = synth.circle(11, 2, 6000, 0.7, 5e-3)
+    opt, ref = _pair(vm, orc, gen, tgt, 0.07, 16, 0, 1.0)
+    i0, j, loss, grad, cnt, ls = opt.Probe(0)
+    g, rcnt, rls = ref.gradient()
+    assert cnt == rcnt
+    assert np.array_equal(grad, g)
+    assert np.float32(ls) == np.float32(rls)
