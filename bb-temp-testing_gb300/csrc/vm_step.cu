@@ -16,133 +16,40 @@
 // the current generators between steps, as the reference rebuilds it at the
 // start of each step.
 #include "vm_device.cuh"
+#include "vm_grid.cuh"
 #include "vm_knn.cuh"
 #include "vm_kernels.h"
 
 namespace vmk {
 
 // ---------------------------------------------------------------------------
-// hash grid build
+// hash grid build over a table of point sets (bodies in vm_grid.cuh)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bin(const VmPointSet *__restrict__ sets, const int *__restrict__ prefix,
                                              int nSets, int emptyIsNegative)
 {
     int f = find_fit(prefix, nSets, blockIdx.x);
-    const VmPointSet &S = sets[f];
-    int i = (blockIdx.x - prefix[f]) * blockDim.x + threadIdx.x;
-    if (i >= S.n) return;
-    float2 p = S.pts[i];
-    // sites: x < 0 is an empty slot (reference binKernel :172); targets: NaN x too (vorolossKernel :216)
-    bool empty = emptyIsNegative ? (p.x < 0.0f) : !(p.x >= 0.0f);
-    if (empty) {
-        S.key[i] = -1;
-        return;
-    }
-    int c = cell_coord(p.y, S.inv, S.gridH) * S.gridW + cell_coord(p.x, S.inv, S.gridW);
-    S.key[i] = c;
-    S.rank[i] = atomicAdd(&S.counts[c], 1);
-}
-
-// block-wide exclusive scan of 8 values per thread (256 threads)
-__device__ __forceinline__ int block_scan8(int (&v)[8], int *warpSums, int &total)
-{
-    int run = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        int x = v[k];
-        v[k] = run;
-        run += x;
-    }
-    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        int t = __shfl_up_sync(kFull, incl, off);
-        if (lane >= off) incl += t;
-    }
-    if (lane == 31) warpSums[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        int w = lane < 8 ? warpSums[lane] : 0, wi = w;
-#pragma unroll
-        for (int off = 1; off < 8; off <<= 1) {
-            int t = __shfl_up_sync(kFull, wi, off);
-            if (lane >= off) wi += t;
-        }
-        if (lane < 8) warpSums[8 + lane] = wi - w;
-        if (lane == 7) warpSums[16] = wi;
-    }
-    __syncthreads();
-    int excl = incl - run + warpSums[8 + warp];
-    total = warpSums[16];
-    return excl;
+    grid_bin_one(sets[f], (blockIdx.x - prefix[f]) * blockDim.x + threadIdx.x, emptyIsNegative);
 }
 
 __global__ void __launch_bounds__(256) k_scan_tiles(const VmPointSet *__restrict__ sets,
                                                     const int *__restrict__ prefix, int nSets)
 {
-    __shared__ int red[8];
     int f = find_fit(prefix, nSets, blockIdx.x);
-    const VmPointSet &S = sets[f];
-    int tile = blockIdx.x - prefix[f];
-    int cells = S.gridW * S.gridH;
-    int base = tile * kScanTile + threadIdx.x * 8;
-    int sum = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (base + k < cells) sum += S.counts[base + k];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(kFull, sum, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int t = 0;
-        for (int w = 0; w < 8; ++w) t += red[w];
-        S.tileSums[tile] = t;
-    }
+    grid_tile_sum(sets[f], blockIdx.x - prefix[f]);
 }
 
 __global__ void __launch_bounds__(256) k_scan_apply(const VmPointSet *__restrict__ sets,
                                                     const int *__restrict__ prefix, int nSets)
 {
-    __shared__ int ws[24];
-    __shared__ int sOffset;
     int f = find_fit(prefix, nSets, blockIdx.x);
-    const VmPointSet &S = sets[f];
-    int tile = blockIdx.x - prefix[f];
-    int cells = S.gridW * S.gridH;
-    // offset of this tile: sum of the earlier tiles' sums
-    int part = 0;
-    for (int t = threadIdx.x; t < tile; t += blockDim.x) part += S.tileSums[t];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) part += __shfl_down_sync(kFull, part, off);
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = part;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int t = 0;
-        for (int w = 0; w < 8; ++w) t += ws[w];
-        sOffset = t;
-    }
-    __syncthreads();
-    int offset = sOffset;
-    int base = tile * kScanTile + threadIdx.x * 8;
-    int v[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = base + k < cells ? S.counts[base + k] : 0;
-    int total;
-    int excl = block_scan8(v, ws, total);
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (base + k < cells) S.start[base + k] = offset + excl + v[k];
-    int tiles = (cells + kScanTile - 1) / kScanTile;
-    if (tile == tiles - 1 && threadIdx.x == 0) S.start[cells] = offset + total;
+    grid_tile_apply(sets[f], blockIdx.x - prefix[f]);
 }
 
 __global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ sets, const int *__restrict__ prefix,
                                                  int nSets, const VmFit *__restrict__ publish)
 {
     int f = find_fit(prefix, nSets, blockIdx.x);
-    const VmPointSet &S = sets[f];
     int local = blockIdx.x - prefix[f];
     if (publish && local == 0 && threadIdx.x == 0 && publish[f].active) {
         // end of a step: publish the loss pass and advance the step counter
@@ -154,36 +61,7 @@ __global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ 
         st->accHi = 0;
         st->accCount = 0;
     }
-    int i = local * blockDim.x + threadIdx.x;
-    if (i >= S.n) return;
-    int c = S.key[i];
-    if (c < 0) return;
-    int s = S.start[c] + S.rank[i];
-    S.outIdx[s] = i;
-    S.outPos[s] = S.pts[i];
-    __threadfence();
-    int left = atomicSub(&S.counts[c], 1); // counts return to zero for the next build
-    if (S.canonical && left == 1) {
-        // last writer of cell c: all writes to its run are visible after the fence
-        __threadfence();
-        int b = S.start[c], e = S.start[c + 1];
-        if (e - b > 1) {
-            for (int a = b + 1; a < e; ++a) {
-                int id = __ldcg(&S.outIdx[a]);
-                float2 ps = __ldcg(&S.outPos[a]);
-                int k = a - 1;
-                while (k >= b) {
-                    int ik = __ldcg(&S.outIdx[k]);
-                    if (ik <= id) break;
-                    S.outIdx[k + 1] = ik;
-                    S.outPos[k + 1] = __ldcg(&S.outPos[k]);
-                    --k;
-                }
-                S.outIdx[k + 1] = id;
-                S.outPos[k + 1] = ps;
-            }
-        }
-    }
+    grid_scatter_one(sets[f], local * blockDim.x + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
