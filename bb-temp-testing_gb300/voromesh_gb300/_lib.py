@@ -88,6 +88,7 @@ SIGNATURES = {
     "vm_get_grid": [P, P, P, P, P],
     "vm_knn": [P, P, I, I, P, P],
     "vm_probe": [P, I, P, P, P, P, P, P],
+    "vm_build_grid_noalloc": [P, I, I, I, F, P, P, P, P],
     "pd_create": [F, F, F, I, C.c_uint, P],
     "pd_destroy": [P],
     "pd_resample": [P, I, I, I, I, P],

@@ -146,6 +146,27 @@ int vm_knn(vm_optimizer *h, const float *queries, int nq, int K, int *idx, float
  * (mode 0). count, lossSum: the pass totals. */
 int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *grad, int *count, float *lossSum);
 
+/* ---- allocation-free hash-grid build --------------------------------------------
+ * No counterpart in the reference. For callers that cannot let a library
+ * allocate device memory (a per-frame edit loop where cudaMalloc's implicit
+ * synchronisation would stall the frame, or a host that plans all device
+ * memory itself): builds the cell-sorted hash grid of `n` generators
+ * (device float2 array, x < 0 = empty slot) into caller-owned device arrays
+ * start (gridW*gridH+1 ints), sortedIdx (n ints) and sortedPos (2n floats),
+ * bit-identical to vm_get_grid's. Nothing is allocated: the scratch lives in
+ * a fixed __device__ array of the library (about 3 MB per device, held until
+ * exit) sized for at most VM_NOALLOC_MAX_POINTS generators and
+ * VM_NOALLOC_MAX_CELLS cells; larger requests return VM_ERR_ARG. Work is
+ * enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream)
+ * and the call returns without waiting. The first call on a device sets up
+ * that device's scratch address; make it before any stream capture. All
+ * calls share the scratch array: calls that overlap on the GPU race, so the
+ * caller must order them (one stream, or events). */
+#define VM_NOALLOC_MAX_POINTS 262144
+#define VM_NOALLOC_MAX_CELLS 262144
+int vm_build_grid_noalloc(const float *generators, int n, int gridW, int gridH, float cellSize, int *start,
+                          int *sortedIdx, float *sortedPos, void *stream);
+
 /* ---- Poisson-disk sampler (poisson::Sampler) ---------------------------------- */
 typedef struct pd_sampler pd_sampler;
 typedef struct {
