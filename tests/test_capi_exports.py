@@ -1,0 +1,66 @@
+"""The C-ABI library loads on a host without a GPU and exports every function
+include/*.h declares (no compute calls)."""
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    from voromesh_gb300 import build as b
+
+    if not b.LIB.exists():
+        b.build()
+    return b.LIB
+
+
+def _declared_c_functions():
+    text = (ROOT / "include" / "vm_capi.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:vm|pd)_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_loads_without_gpu(libpath):
+    import ctypes
+
+    lib = ctypes.CDLL(str(libpath))
+    lib.vm_error_string.restype = ctypes.c_char_p
+    assert lib.vm_error_string(0) == b"ok"
+
+
+def test_every_c_function_is_exported(libpath):
+    import ctypes
+
+    lib = ctypes.CDLL(str(libpath))
+    names = _declared_c_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_cpp_classes_are_exported(libpath):
+    out = subprocess.run(["nm", "-DC", "--defined-only", str(libpath)], capture_output=True, text=True).stdout
+    for sym in ["voromesh::VoroOptimizer::VoroOptimizer(float, float, float, voromesh::OptimizerParams const&)",
+                "voromesh::VoroOptimizer::SetTargets(std::vector<voromesh::Vec2, std::allocator<voromesh::Vec2> > const&)",
+                "voromesh::VoroOptimizer::Step(int)", "voromesh::VoroOptimizer::EvaluateLoss()",
+                "voromesh::VoroOptimizer::Extract()", "voromesh::VoroOptimizer::BeginSchedule(int, int, int, int, int)",
+                "poisson::Sampler::Sampler(float, float, float, int, unsigned int)",
+                "poisson::Sampler::Resample(int, int, int, int)", "poisson::Sampler::Verify(int, int, int, int) const",
+                "voromesh::SetDefaultLossNeighbours(int)"]:
+        assert sym in out, sym
+
+
+def test_status_codes_without_gpu(libpath):
+    """Argument checks answer before any device call."""
+    import ctypes as C
+
+    lib = C.CDLL(str(libpath))
+    assert lib.vm_create(C.c_float(-1.0), C.c_float(1.0), C.c_float(0.1), None, C.byref(C.c_void_p())) == 1
+    assert lib.pd_create(C.c_float(1.0), C.c_float(1.0), C.c_float(0.0), 30, 1, C.byref(C.c_void_p())) == 1
+    buf = C.create_string_buffer(256)
+    assert lib.vm_last_error(buf, 256) == 0 and len(buf.value) > 0

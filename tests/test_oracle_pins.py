@@ -1,0 +1,159 @@
+"""The oracle against golden vectors of the reference's own kernels.
+
+tests/golden/reference_kernels.npz was produced by tests/golden/make_golden.py
+from the reference's kernel code compiled for the CPU (oracle/ref_shim). The
+oracle's reference mode (float sums in target order, powf) must reproduce
+every array bit for bit; its fixed-point mode (the product's arithmetic) must
+stay within the stated tolerances.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLD = Path(__file__).resolve().parent / "golden" / "reference_kernels.npz"
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+@pytest.fixture(scope="module")
+def plain():
+    from voromesh_gb300 import synth
+
+    return synth.plain_fit()
+
+
+def test_inputs_regenerate(plain, gold):
+    # the fixtures' inputs come from the seeded generators; their grid pins them
+    from oracle import oracle as orc
+
+    st, si, sp, gc = orc.build_grid(plain.generators, 40, 40, 0.05)
+    assert np.array_equal(st, gold["plain_grid_start"])
+    assert np.array_equal(si, gold["plain_grid_idx"])
+    assert np.array_equal(sp, gold["plain_grid_pos"])
+    assert np.array_equal(gc, gold["plain_grid_cell"])
+
+
+@pytest.mark.parametrize("K", [12, 16, 32])
+def test_knn_lists(orc, plain, gold, K):
+    grid = orc.Grid(plain.generators, 40, 40, 0.05)
+    idx, d2 = grid.knn(plain.targets[:512], K)
+    assert np.array_equal(idx, gold[f"plain_knn{K}_idx"])
+    assert np.array_equal(d2, gold[f"plain_knn{K}_d2"])
+
+
+def test_knn_matches_brute_force(orc, plain):
+    import ctypes as C
+
+    grid = orc.Grid(plain.generators, 40, 40, 0.05)
+    q = plain.targets[:200]
+    idx, d2 = grid.knn(q, 16)
+    L = orc.lib()
+    g = np.ascontiguousarray(plain.generators)
+    for i in range(len(q)):
+        bi = np.empty(16, np.int32)
+        bd = np.empty(16, np.float32)
+        L.vo_knn_brute(orc.P(g), len(g), orc.VoF2(q[i, 0], q[i, 1]), 16, C.c_void_p(bi.ctypes.data),
+                       C.c_void_p(bd.ctypes.data))
+        assert np.array_equal(bi, idx[i]) and np.array_equal(bd, d2[i])
+
+
+def _ref_fit(orc, plain, fraction, acc, pw, K=12):
+    f = orc.Fit(2.0, 2.0, 0.05, K, plain.lrPerSpacing, fraction, 300, acc=acc, pow_mode=pw)
+    f.set_targets(plain.targets)
+    f.set_generators(plain.generators, 2048, 1, 2.0)
+    return f
+
+
+def test_first_gradient(orc, plain, gold):
+    f = _ref_fit(orc, plain, 1.0, orc.ACC_REF, orc.POW_REF)
+    g, cnt, loss = f.gradient()
+    assert cnt == int(gold["plain_step1_count"][0])
+    assert np.float32(loss) == gold["plain_step1_loss"][0]
+    assert np.array_equal(g, gold["plain_step1_grad"])
+
+
+@pytest.mark.parametrize("fraction", [1.0, 0.2])
+def test_forty_steps(orc, plain, gold, fraction):
+    key = f"plain_f{int(fraction * 100)}"
+    f = _ref_fit(orc, plain, fraction, orc.ACC_REF, orc.POW_REF)
+    losses = [f.step(1) for _ in range(40)]
+    g, m, v = f.generators()
+    assert np.array_equal(np.float32(losses), gold[f"{key}_losses"])
+    assert np.array_equal(g, gold[f"{key}_gen"])
+    assert np.array_equal(m, gold[f"{key}_m"]) and np.array_equal(v, gold[f"{key}_v"])
+
+
+def test_k16_gradient(orc, gold):
+    from voromesh_gb300 import synth
+
+    f = orc.Fit(2.0, 2.0, 0.06, 16, 0.09, 1.0, 300, acc=orc.ACC_REF, pow_mode=orc.POW_REF)
+    f.set_targets(synth.circle(3, 2, 8192, 0.6, 1e-3))
+    f.set_generators(synth.uniform(3, 1, 1024), 1024, 1, 2.0)
+    g, cnt, loss = f.gradient()
+    assert cnt == int(gold["k16_count"][0])
+    assert np.float32(loss) == gold["k16_loss"][0]
+    assert np.array_equal(g, gold["k16_grad"])
+
+
+def test_fixed_point_mode_tolerance(orc, plain, gold):
+    """The product's sums (exact fixed point) vs the reference's float sums:
+    the first gradient within 1e-5 of the gradient's scale (max |g|) and at
+    least as close to the FP64 oracle as the reference's float sum is; loss
+    within 1e-5 relative; positions after 5 steps within 1e-5 of the domain
+    extent. (The reference's own float-atomic order varies by more than that
+    over longer horizons.)"""
+    fx = _ref_fit(orc, plain, 1.0, orc.ACC_FIXED, orc.POW_DET)
+    g, cnt, loss = fx.gradient()
+    gref = gold["plain_step1_grad"]
+    assert cnt == int(gold["plain_step1_count"][0])
+    assert abs(loss - gold["plain_step1_loss"][0]) <= 1e-5 * abs(gold["plain_step1_loss"][0])
+    assert np.abs(g - gref).max() <= 1e-5 * np.abs(gref).max()
+    d = orc.Fit64(2.0, 2.0, float(np.float32(0.05)), 12, plain.lrPerSpacing, 1.0, 300)
+    d.set_targets(plain.targets)
+    d.set_generators(plain.generators, 2048, 1, 2.0)
+    g64, _, _ = d.gradient()
+    assert np.abs(g - g64).max() <= np.abs(gref - g64).max()
+    rf = _ref_fit(orc, plain, 1.0, orc.ACC_REF, orc.POW_REF)
+    fx.step(5)
+    rf.step(5)
+    assert np.abs(fx.generators()[0] - rf.generators()[0]).max() <= 2e-5
+
+
+def test_fp64_error_bar(orc, plain):
+    """FP32 arithmetic vs the FP64 oracle after 10 steps (reported, bounded)."""
+    fx = _ref_fit(orc, plain, 1.0, orc.ACC_FIXED, orc.POW_DET)
+    d = orc.Fit64(2.0, 2.0, float(np.float32(0.05)), 12, plain.lrPerSpacing, 1.0, 300)
+    d.set_targets(plain.targets)
+    d.set_generators(plain.generators, 2048, 1, 2.0)
+    fx.step(10)
+    d.step(10)
+    err = np.abs(fx.generators()[0].astype(np.float64) - d.generators()).max()
+    assert err < 1e-3  # a few lr; bisector flips between FP32 and FP64 are discrete
+
+
+def test_cells(orc, gold):
+    from voromesh_gb300 import synth
+
+    gen = synth.uniform(8, 1, 300)
+    gen[::17] = -1.0
+    grid = orc.Grid(gen, 17, 17, 0.12)
+    verts, edges, counts, inside, flags = grid.cells(2.0, 2.0, gold["cells_masks"], 4, 4, 16.0)
+    assert np.array_equal(counts, gold["cells_counts"])
+    assert np.array_equal(inside, gold["cells_inside"])
+    assert np.array_equal(flags, gold["cells_flags"])
+    for i in range(len(gen)):
+        c = counts[i]
+        assert np.array_equal(edges[i, :c], gold["cells_edges"][i, :c])
+        assert np.array_equal(verts[i, :c], gold["cells_verts"][i, :c])
+
+
+def test_poisson(orc, gold):
+    grid, p = orc.poisson_fill(1.0, 1.0, 0.02, 30, 1)
+    assert np.array_equal(grid, gold["poisson_fill"])
+    assert orc.poisson_verify(p, grid, 0, 0, p.gridW, p.gridH)
+    grid, p = orc.poisson_fill(1.0, 1.0, 0.02, 30, 1, [(5, 5, 17, 13), (0, 0, 3, 40), (30, 30, 80, 80)])
+    assert np.array_equal(grid, gold["poisson_regions"])
