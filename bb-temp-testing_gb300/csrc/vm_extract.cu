@@ -219,7 +219,57 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
     if (!certified && beyond(d2[kCellK - 1], *P)) certified = true;
     if (!certified) {
         atomicAdd(&flags[0], 1);
-        for (int j = 0; j < F.nSlots; ++j) {
+        // The reference clips by every other generator in index order, skipping
+        // those beyond the current security radius (:402-414). Only sites within
+        // the radius at this point can cut the cell (r2max only shrinks), so they
+        // are gathered from the hash grid, sorted by index and clipped in that
+        // order -- the same sequence of cuts. Too many candidates: the full loop.
+        constexpr int kGather = 256;
+        int cand[kGather];
+        int nc = 0;
+        bool gathered = true;
+        double R2 = 4.0 * r2max_d(*P);
+        float R = (float)sqrt(R2) * 1.0001f + 1e-30f;
+        int gx0 = cell_coord(ci.x - R, F.inv, F.gridW), gx1 = cell_coord(ci.x + R, F.inv, F.gridW);
+        int gy0 = cell_coord(ci.y - R, F.inv, F.gridH), gy1 = cell_coord(ci.y + R, F.inv, F.gridH);
+        if ((long long)(gx1 - gx0 + 1) * (gy1 - gy0 + 1) > 4096) gathered = false;
+        for (int gy = gy0; gathered && gy <= gy1; ++gy) {
+            int s0 = F.start[gy * F.gridW + gx0], s1 = F.start[gy * F.gridW + gx1 + 1];
+            for (int s = s0; s < s1; ++s) {
+                int j = F.sortedIdx[s];
+                if (j == i) continue;
+                bool seen = false;
+                for (int k = 0; k < kCellK; ++k) seen |= idx[k] == j;
+                if (seen) continue;
+                float2 g = F.sortedPos[s];
+                double rx = (double)g.x - (double)ci.x, ry = (double)g.y - (double)ci.y;
+                if (rx * rx + ry * ry > R2) continue;
+                if (nc == kGather) {
+                    gathered = false;
+                    break;
+                }
+                int k = nc++;
+                while (k > 0 && cand[k - 1] > j) {
+                    cand[k] = cand[k - 1];
+                    --k;
+                }
+                cand[k] = j;
+            }
+        }
+        if (gathered) {
+            for (int q = 0; q < nc; ++q) {
+                int j = cand[q];
+                float2 g = F.gen[j];
+                double rx = (double)g.x - (double)ci.x, ry = (double)g.y - (double)ci.y;
+                if (rx * rx + ry * ry > 4.0 * r2max_d(*P)) continue;
+                bool changed;
+                ok &= clip(c, *P, *Q, j, g, changed);
+                if (changed) {
+                    CellPoly *t = P; P = Q; Q = t;
+                }
+            }
+        }
+        for (int j = 0; !gathered && j < F.nSlots; ++j) {
             if (j == i) continue;
             float2 g = F.gen[j];
             if (g.x < 0.0f) continue;

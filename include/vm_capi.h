@@ -146,6 +146,77 @@ int vm_knn(vm_optimizer *h, const float *queries, int nq, int K, int *idx, float
  * (mode 0). count, lossSum: the pass totals. */
 int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *grad, int *count, float *lossSum);
 
+/* ---- batched fits --------------------------------------------------------------
+ * No counterpart in the reference, which runs one VoroOptimizer at a time
+ * (apps/voromesh_demo.cpp:103-156). A batch holds independent fits of any
+ * sizes in one device arena (its size is the HBM budget) and steps all of
+ * them together: each stage of a step is one launch over all live fits.
+ * A fit's results do not depend on the other fits in the batch (exact
+ * fixed-point sums), so they equal what a VoroOptimizer computes alone. */
+typedef struct vmb_batch vmb_batch;
+typedef struct {
+    float width, height, spacing; /* VoroOptimizer(width, height, spacing, params) */
+    vm_params params;             /* the schedule is BeginSchedule(params.iterations) over all slots */
+    const float *generators;      /* SetGenerators(generators, slotsW, slotsH, slotCellSize) */
+    int slotsW, slotsH;
+    float slotCellSize;
+    const float *targets;         /* SetTargets(targets[0..nTargets)) */
+    int nTargets;
+} vmb_fit;
+typedef struct {
+    int iteration;   /* steps taken */
+    float lastLoss;  /* loss / count of the last published pass */
+    int numSlots, liveTargets, active;
+} vmb_fit_info_t;
+
+int vmb_create(size_t arenaBytes, int maxFits, int lossVariant, vmb_batch **out);
+int vmb_destroy(vmb_batch *b);
+/* Arena bytes a fit of this shape needs (admission control). */
+size_t vmb_fit_bytes(int slotsW, int slotsH, int nTargets, float width, float height, float spacing);
+/* Uploads a fit (copies the host buffers); VM_ERR_BUDGET when it does not fit the arena. */
+int vmb_add_fit(vmb_batch *b, const vmb_fit *fit, int *fitId);
+int vmb_remove_fit(vmb_batch *b, int fitId);
+/* Inactive fits keep their memory but are not stepped. */
+int vmb_set_active(vmb_batch *b, int fitId, int active);
+/* `iterations` steps of every active fit; GPU ms of the whole run. */
+int vmb_step(vmb_batch *b, int iterations, float *gpuMs);
+/* EvaluateLoss() of every active fit; losses[fitId] (maxFits entries). */
+int vmb_evaluate(vmb_batch *b, float *losses);
+int vmb_fit_info(vmb_batch *b, int fitId, vmb_fit_info_t *out);
+int vmb_get_generators(vmb_batch *b, int fitId, float *xy);
+int vmb_memory(vmb_batch *b, size_t *freeBytes, size_t *totalBytes, int *liveFits);
+
+/* ---- serving: continuous batching of arriving fit requests -----------------------
+ * Requests become visible at their arrival time (seconds after the call
+ * starts). Arrived requests are admitted in arrival order while the HBM
+ * budget and `maxLive` allow; all live fits step together, `stepsPerRound`
+ * steps at a time; after each round every live fit's full-target loss is
+ * evaluated and the fit retires when it has taken maxSteps steps or its
+ * loss changed by less than relTol (relative) since the previous round. A
+ * retired fit's generators are copied to outGenerators (when non-NULL) and
+ * its memory admits the next request. maxLive = 1 is the one-fit-at-a-time
+ * loop. Times in vms_result are seconds since the call started. */
+typedef struct {
+    double arrival;
+    vmb_fit fit;
+    int maxSteps;
+    float relTol;
+    float *outGenerators; /* slotsW*slotsH (x,y) pairs, or NULL */
+} vms_request;
+typedef struct {
+    size_t hbmBudgetBytes;
+    int maxLive;
+    int stepsPerRound;
+    int lossVariant; /* -1 = default */
+} vms_config;
+typedef struct {
+    double arrival, admitted, finished;
+    int steps;
+    float finalLoss;
+    int status; /* VM_OK, or VM_ERR_BUDGET when the fit can never fit */
+} vms_result;
+int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result *results);
+
 /* ---- allocation-free hash-grid build --------------------------------------------
  * No counterpart in the reference. For callers that cannot let a library
  * allocate device memory (a per-frame edit loop where cudaMalloc's implicit

@@ -1,0 +1,88 @@
+"""Batched fits and serving: every fit's result equals the same fit run alone
+(bit for bit), in a batch of uneven sizes and in the served mix."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(n_fits=12, seed=3):
+    from voromesh_gb300 import synth
+
+    return synth.uneven_batch(n_fits=n_fits, lo=200, hi=6000, tgt_per_gen=4, steps=30, seed=seed)
+
+
+def alone(spec, steps):
+    import voromesh_gb300 as vm
+    from voromesh_gb300.batch import params_for
+
+    o = vm.VoroOptimizer(spec.width, spec.height, spec.spacing, params_for(spec))
+    o.SetTargets(spec.targets)
+    o.SetGenerators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
+    o.Step(steps)
+    g = o.Generators()
+    o.close()
+    return g
+
+
+def test_batch_equals_alone(vm):
+    from voromesh_gb300.batch import Batch
+
+    specs = small_batch()
+    b = Batch(1 << 30, max_fits=64)
+    ids = [b.add(s) for s in specs]
+    b.step(30)
+    for fid, spec in zip(ids, specs):
+        assert b.info(fid).iteration == 30
+        assert np.array_equal(b.generators(fid), alone(spec, 30))
+    b.close()
+
+
+def test_batch_membership_changes(vm):
+    """Fits join and leave between steps; the others are unaffected."""
+    from voromesh_gb300.batch import Batch
+
+    specs = small_batch(6, seed=4)
+    b = Batch(1 << 30, max_fits=16)
+    a = [b.add(s) for s in specs[:3]]
+    b.step(10)
+    b.remove(a[1])
+    c = [b.add(s) for s in specs[3:]]
+    b.step(10)
+    assert np.array_equal(b.generators(a[0]), alone(specs[0], 20))
+    assert np.array_equal(b.generators(a[2]), alone(specs[2], 20))
+    for fid, spec in zip(c, specs[3:]):
+        assert np.array_equal(b.generators(fid), alone(spec, 10))
+    b.close()
+
+
+def test_budget_admission(vm):
+    from voromesh_gb300.batch import Batch, fit_bytes
+    from voromesh_gb300._lib import VmError
+
+    specs = small_batch(4, seed=5)
+    need = max(fit_bytes(s) for s in specs)
+    b = Batch(int(need * 1.5), max_fits=8)
+    b.add(specs[0])
+    with pytest.raises(VmError) as e:
+        for s in specs[1:]:
+            b.add(s)
+    assert e.value.code == 5  # VM_ERR_BUDGET
+    b.close()
+
+
+def test_serve_equals_alone(vm):
+    """Served results (continuous batching, staggered arrivals) equal each
+    request run alone for the same number of steps."""
+    from voromesh_gb300.batch import serve
+
+    specs = small_batch(8, seed=6)
+    arrivals = np.linspace(0.0, 0.05, len(specs))
+    r = serve(specs, arrivals, hbm_budget=1 << 30, max_live=64, steps_per_round=10, max_steps=40, rel_tol=0.0)
+    assert np.all(r.status == 0) and np.all(r.steps == 40)
+    assert np.all(r.finished >= r.arrival)
+    for spec, g in zip(specs, r.generators):
+        assert np.array_equal(g, alone(spec, 40))
+    one = serve(specs, arrivals, hbm_budget=1 << 30, max_live=1, steps_per_round=10, max_steps=40, rel_tol=0.0)
+    for g1, g2 in zip(one.generators, r.generators):
+        assert np.array_equal(g1, g2)
