@@ -50,10 +50,17 @@ KERNELS_PER_STEP = 6  # k_loss, k_loss_exact, k_adam_bin, k_scan_tiles, k_scan_a
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve"],
+                    help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads")
+    ap.add_argument("--fits", type=int, default=512)
+    ap.add_argument("--fit-steps", type=int, default=200)
+    ap.add_argument("--requests", type=int, default=200)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--serve-budget-gb", type=int, default=64)
     return ap.parse_args()
 
 
@@ -187,11 +194,111 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def pct(a, q):
+    return float(np.percentile(np.asarray(a), q)) if len(a) else None
+
+
+def run_batch(args):
+    """Uneven batch: 512 fits (generators log-uniform in [1,024, 262,144], 4x
+    targets on random star polygons, 200 steps each) in one batch, against the
+    one-fit-at-a-time loop on the same GPU. fits/s over uploads + steps."""
+    import voromesh_gb300 as vm
+    from voromesh_gb300 import synth
+    from voromesh_gb300.batch import Batch, fit_bytes, params_for
+
+    specs = synth.uneven_batch(n_fits=args.fits, steps=args.fit_steps)
+    total_sites = sum(s.slotsW * s.slotsH for s in specs)
+    arena = int(sum(fit_bytes(s) for s in specs) * 1.05) + (64 << 20)
+    # warm-up: one small batch (module load, tables)
+    w = Batch(256 << 20, max_fits=4)
+    w.add(specs[0])
+    w.step(3)
+    w.close()
+    t0 = time.perf_counter()
+    b = Batch(arena, max_fits=len(specs))
+    for s in specs:
+        b.add(s)
+    t1 = time.perf_counter()
+    gpu_ms = b.step(args.fit_steps)
+    losses = b.evaluate()
+    t2 = time.perf_counter()
+    b.close()
+    batched = {"fits_per_s": len(specs) / (t2 - t0), "wall_s": t2 - t0, "upload_s": t1 - t0,
+               "step_gpu_ms": gpu_ms, "site_steps_per_s": total_sites * args.fit_steps / (gpu_ms / 1e3)}
+    # plain loop: one VoroOptimizer at a time, each graph-stepped (the reference's usage pattern)
+    t0 = time.perf_counter()
+    gpu_plain = 0.0
+    for s in specs:
+        o = vm.VoroOptimizer(s.width, s.height, s.spacing, params_for(s))
+        o.SetTargets(s.targets)
+        o.SetGenerators(s.generators, s.slotsW, s.slotsH, s.slotCellSize)
+        gpu_plain += o.Step(args.fit_steps)
+        o.close()
+    t1 = time.perf_counter()
+    plain = {"fits_per_s": len(specs) / (t1 - t0), "wall_s": t1 - t0, "step_gpu_ms": gpu_plain}
+    print(json.dumps({"metric": "fits/s, uneven batch", "workload": f"{len(specs)} fits, generators log-uniform "
+                      f"[1024, 262144] (sum {total_sites}), 4x targets on random stars, {args.fit_steps} steps each, k=16",
+                      "batched": batched, "plain_loop": plain, "speedup": batched["fits_per_s"] / plain["fits_per_s"],
+                      "unit": "fits/s", "data": "synthetic"}), flush=True)
+
+
+def run_serve(args):
+    """Served stream: Poisson arrivals, generators log-uniform in [1k, 1M],
+    8x targets from the ellipse-union or star shapes (coin flip), retire at
+    500 steps or relative loss change < 1e-6; continuous batching vs the
+    one-fit-at-a-time loop; fits/s and p50/p99 arrival-to-result latency."""
+    import concurrent.futures as cf
+    import math
+
+    from voromesh_gb300 import synth
+    from voromesh_gb300.batch import fit_bytes, serve
+
+    n = args.requests
+    arrivals = synth.arrival_times(1, n, args.rate)
+    sizes = synth.log_uniform_ints(1, 17, n, 1024, 1048576)
+    coin = synth.uniform01(1, 19, n)
+    pool_n = int(8 * sizes.max())
+    # shape pools, generated in parallel (the generators release the GIL)
+    with cf.ThreadPoolExecutor(8) as ex:
+        fut = [ex.submit(synth.ellipse_union, 1, 800 + k, pool_n, 64) for k in range(2)]
+        fut += [ex.submit(synth.random_star, 1, 900 + 2 * k, pool_n) for k in range(4)]
+        pools = [f.result() for f in fut]
+    specs = []
+    for i in range(n):
+        s = int(sizes[i])
+        pool = pools[i % 2] if coin[i] < 0.5 else pools[2 + i % 4]
+        off = (i * 7919) % max(1, len(pool) - 8 * s)
+        tgt = np.ascontiguousarray(pool[off:off + 8 * s])
+        gen = synth.uniform(1, 600000 + 3 * i, s)
+        specs.append(synth.FitSpec(f"req_{i}", 2.0, 2.0, 2.0 / math.sqrt(s), gen, s, 1, 2.0, tgt, 16, 0.09, 500))
+    budget = args.serve_budget_gb << 30
+    need = max(fit_bytes(s) for s in specs)
+    out = {}
+    for name, live in (("batched", 4096), ("plain_loop", 1)):
+        r = serve(specs, arrivals, budget, max_live=live, steps_per_round=10, max_steps=500, rel_tol=1e-6,
+                  keep_generators=False)
+        lat = r.latency
+        span = float(r.finished.max() - r.arrival.min())
+        out[name] = {"fits_per_s": n / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99), "span_s": span,
+                     "mean_steps": float(r.steps.mean()), "rejected": int((r.status != 0).sum())}
+    print(json.dumps({"metric": "fits/s + p50/p99, served stream", "workload": f"{n} requests, Poisson arrivals "
+                      f"{args.rate}/s, generators log-uniform [1k, 1M], 8x targets (ellipse union or star), retire at "
+                      f"500 steps or rel loss change < 1e-6, HBM budget {args.serve_budget_gb} GiB", **out,
+                      "speedup": out["batched"]["fits_per_s"] / out["plain_loop"]["fits_per_s"],
+                      "largest_fit_bytes": need, "unit": "fits/s", "data": "synthetic"}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "batch":
+        run_batch(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
     import torch
 
