@@ -186,4 +186,14 @@ __device__ __forceinline__ int find_fit(const int *prefix, int nFits, int b)
     return lo;
 }
 
+// Targets the loss kernel's block certificates could not settle are deferred
+// to this queue and resolved by k_loss_exact in dense warps, so one hard
+// target does not stall the 31 other lanes of its warp on the long ring
+// search. The queue holds every live target, so it cannot overflow.
+struct SlowQueue {
+    int count;
+    int capacity;
+    int2 *items; // (fit, local target index)
+};
+
 } // namespace vmk

@@ -8,6 +8,9 @@
 
 namespace vmk {
 
+// Keys of a point set: its grid cells, times the sub-cells of each.
+__device__ __forceinline__ int grid_keys(const VmPointSet &S) { return (S.gridW * S.gridH) << (2 * S.sub); }
+
 // cell key + atomic rank of point i. Sites: x < 0 is an empty slot
 // (reference binKernel :172); targets: NaN x too (vorolossKernel :216).
 __device__ __forceinline__ void grid_bin_one(const VmPointSet &S, int i, int emptyIsNegative)
@@ -19,7 +22,17 @@ __device__ __forceinline__ void grid_bin_one(const VmPointSet &S, int i, int emp
         S.key[i] = -1;
         return;
     }
-    int c = cell_coord(p.y, S.inv, S.gridH) * S.gridW + cell_coord(p.x, S.inv, S.gridW);
+    int c;
+    if (S.sub) {
+        // cell-major key with the sub-cell (row-major within the cell) below it;
+        // scaling inv by 2^sub is exact, so key >> 2 sub is the cell itself
+        int fx = cell_coord(p.x, S.inv * (float)(1 << S.sub), S.gridW << S.sub);
+        int fy = cell_coord(p.y, S.inv * (float)(1 << S.sub), S.gridH << S.sub);
+        int m = (1 << S.sub) - 1;
+        c = ((((fy >> S.sub) * S.gridW + (fx >> S.sub)) << S.sub | (fy & m)) << S.sub) | (fx & m);
+    } else {
+        c = cell_coord(p.y, S.inv, S.gridH) * S.gridW + cell_coord(p.x, S.inv, S.gridW);
+    }
     S.key[i] = c;
     S.rank[i] = atomicAdd(&S.counts[c], 1);
 }
@@ -63,7 +76,7 @@ __device__ __forceinline__ int block_scan8(int (&v)[8], int *warpSums, int &tota
 __device__ __forceinline__ void grid_tile_sum(const VmPointSet &S, int tile)
 {
     __shared__ int red[8];
-    int cells = S.gridW * S.gridH;
+    int cells = grid_keys(S);
     int base = tile * kScanTile + threadIdx.x * 8;
     int sum = 0;
 #pragma unroll
@@ -85,7 +98,7 @@ __device__ __forceinline__ void grid_tile_apply(const VmPointSet &S, int tile)
 {
     __shared__ int ws[24];
     __shared__ int sOffset;
-    int cells = S.gridW * S.gridH;
+    int cells = grid_keys(S);
     int part = 0;
     for (int t = threadIdx.x; t < tile; t += blockDim.x) part += S.tileSums[t];
 #pragma unroll

@@ -157,6 +157,8 @@ struct vm_optimizer {
     DevBuf<VmFit> dFit;
     DevBuf<VmPointSet> dSites, dTargets;
     DevBuf<int> dPre; // [0, siteBlocks, 0, tiles, 0, lossTiles, 0, targetBlocks]
+    DevBuf<int> dTPre; // [0, targetBlocks, 0, targetKeyTiles]
+    DevBuf<int> tcounts, tstart, ttileSums; // target sort by sub-cell (only while sorting)
     DevBuf<char> queue;  // deferred-target queue header
     DevBuf<int2> qitems; // its items
     std::vector<cudaEvent_t> timing; // vm_step_timed events
@@ -200,15 +202,11 @@ int upload_tables(vm_optimizer *h)
     S.pts = h->gen.p; S.n = n; S.gridW = h->gridW; S.gridH = h->gridH; S.inv = F.inv;
     S.key = h->key.p; S.rank = h->rank.p; S.counts = h->counts.p; S.start = h->start.p; S.tileSums = h->tileSums.p;
     S.outPos = h->sortedPos.p; S.outIdx = h->sortedIdx.p; S.canonical = 1; S.useIndexOrder = 1;
-    VmPointSet T = S;
-    T.pts = h->traw.p; T.n = h->targetCapacity; T.key = h->tkey.p; T.rank = h->trank.p;
-    T.outPos = h->tpos.p; T.outIdx = h->tslot.p; T.canonical = 0;
     int pre[8] = {0, (n + 255) / 256, 0, h->tiles, 0, (h->liveTargets + h->lossTile - 1) / h->lossTile, 0,
                   (h->targetCapacity + 255) / 256};
     cudaError_t e;
     if ((e = cudaMemcpyAsync(h->dFit.p, &F, sizeof(VmFit), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload fit");
     if ((e = cudaMemcpyAsync(h->dSites.p, &S, sizeof(S), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload sites");
-    if ((e = cudaMemcpyAsync(h->dTargets.p, &T, sizeof(T), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload targets");
     if ((e = cudaMemcpyAsync(h->dPre.p, pre, sizeof(pre), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload prefix");
     // the tables live in pageable memory on the host: finish before they change
     if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "upload sync");
@@ -230,7 +228,7 @@ void choose_loss_variant(vm_optimizer *h, int sms)
         const char *env = std::getenv("VM_LOSS_VARIANT");
         if (env && *env) v = std::atoi(env);
     }
-    if (v < 0 || v >= vm_loss_variants()) v = h->liveTargets < 256 * 4 * sms ? 7 : 3;
+    if (v < 0 || v >= vm_loss_variants()) v = h->liveTargets < 256 * 4 * sms ? 5 : 1;
     h->lossVariant = v;
     h->lossTile = vm_loss_variant_threads(v);
     h->lossGrid = vm_loss_occupancy_blocks(v);
@@ -295,19 +293,53 @@ int read_state(vm_optimizer *h, VmState &st)
     return VM_OK;
 }
 
+// log2 of the sub-cells per cell side in the target order: 4x4 sub-cells keep
+// each warp's 32 targets in a small box (tight distance bounds in the loss),
+// within 2^27 sort keys. VM_TARGET_SUB overrides it (0-3).
+int target_sub(const vm_optimizer *h)
+{
+    int sub = 2;
+    const char *env = std::getenv("VM_TARGET_SUB");
+    if (env && *env) sub = std::min(std::max(std::atoi(env), 0), 3);
+    while (sub > 0 && ((long long)h->cells << (2 * sub)) > (1LL << 27)) --sub;
+    return sub;
+}
+
+// Targets in (cell, sub-cell) order, the order the loss pass walks them. The
+// key arrays exist only during the sort.
 int sort_targets(vm_optimizer *h)
 {
     cudaError_t e;
+    int rc;
+    int sub = target_sub(h);
+    long long keys = (long long)h->cells << (2 * sub);
+    int keyTiles = (int)((keys + kScanTile - 1) / kScanTile);
     int tb = (h->targetCapacity + 255) / 256;
-    if ((e = vm_launch_bin(h->dTargets.p, h->dPre.p + 6, 1, tb, 0, h->stream))) return cuda_fail(e, "target bin");
-    if ((e = vm_launch_scan(h->dTargets.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "target scan");
-    if ((e = vm_launch_scatter(h->dTargets.p, h->dPre.p + 6, 1, tb, nullptr, h->stream)))
+    if ((rc = h->tcounts.alloc(keys + 1)) || (rc = h->tstart.alloc(keys + 1)) ||
+        (rc = h->ttileSums.alloc(keyTiles + 1)))
+        return rc;
+    VmPointSet T{};
+    T.pts = h->traw.p; T.n = h->targetCapacity; T.gridW = h->gridW; T.gridH = h->gridH; T.inv = 1.0f / h->spacing;
+    T.key = h->tkey.p; T.rank = h->trank.p; T.counts = h->tcounts.p; T.start = h->tstart.p;
+    T.tileSums = h->ttileSums.p; T.outPos = h->tpos.p; T.outIdx = h->tslot.p; T.canonical = 0; T.useIndexOrder = 1;
+    T.sub = sub;
+    int pre[4] = {0, tb, 0, keyTiles};
+    if ((e = cudaMemsetAsync(h->tcounts.p, 0, sizeof(int) * (size_t)(keys + 1), h->stream)) ||
+        (e = cudaMemcpyAsync(h->dTargets.p, &T, sizeof(T), cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->dTPre.p, pre, sizeof(pre), cudaMemcpyHostToDevice, h->stream)))
+        return cuda_fail(e, "target sort tables");
+    if ((e = vm_launch_bin(h->dTargets.p, h->dTPre.p, 1, tb, 0, h->stream))) return cuda_fail(e, "target bin");
+    if ((e = vm_launch_scan(h->dTargets.p, h->dTPre.p + 2, 1, keyTiles, h->stream))) return cuda_fail(e, "target scan");
+    if ((e = vm_launch_scatter(h->dTargets.p, h->dTPre.p, 1, tb, nullptr, h->stream)))
         return cuda_fail(e, "target scatter");
     int live = 0;
-    if ((e = cudaMemcpyAsync(&live, h->start.p + h->cells, sizeof(int), cudaMemcpyDeviceToHost, h->stream)))
+    if ((e = cudaMemcpyAsync(&live, h->tstart.p + keys, sizeof(int), cudaMemcpyDeviceToHost, h->stream)))
         return cuda_fail(e, "live targets");
+    // the tables above live on the host stack
     if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "target sort");
-    h->gridValid = false; // the grid buffers were borrowed
+    h->tcounts.release();
+    h->tstart.release();
+    h->ttileSums.release();
     if (live != h->liveTargets) drop_graph(h);
     h->liveTargets = live;
     int qcap = std::max(live, 1); // every live target fits: the loss never overflows the queue
@@ -315,7 +347,6 @@ int sort_targets(vm_optimizer *h)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     choose_loss_variant(h, sms);
-    int rc;
     if ((rc = h->qitems.reserve(qcap))) return rc;
     if ((e = vm_queue_init(h->queue.p, h->qitems.p, qcap, h->stream))) return cuda_fail(e, "queue");
     return upload_tables(h);
@@ -409,6 +440,7 @@ int vm_create(float width, float height, float spacing, const vm_params *params,
     if (!rc) rc = h->dSites.alloc(1);
     if (!rc) rc = h->dTargets.alloc(1);
     if (!rc) rc = h->dPre.alloc(8);
+    if (!rc) rc = h->dTPre.alloc(4);
     if (!rc) rc = h->flags.alloc(2);
     if (!rc) rc = h->queue.alloc(vm_queue_bytes());
     if (!rc && (e = vm_queue_init(h->queue.p, nullptr, 0, h->stream))) rc = cuda_fail(e, "queue");

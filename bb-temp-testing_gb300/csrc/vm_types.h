@@ -82,6 +82,7 @@ struct VmPointSet {
     int *outIdx;
     int canonical; // sort each cell's run by index after the scatter
     int useIndexOrder; // outIdx holds the source index (always 1 today)
+    int sub;           // log2 of the sub-cells per cell side in the sort key (targets; 0 for sites)
 };
 
 constexpr int kScanTile = 2048; // cells per scan tile (256 threads x 8)

@@ -105,3 +105,23 @@ def test_probe_matches_oracle(vm, orc):
     assert cnt == rcnt
     assert np.array_equal(grad, g)
     assert np.float32(ls) == np.float32(rls)
+
+
+@pytest.mark.parametrize("sub", ["0", "2"])
+def test_loss_variants_and_target_order_agree(vm, orc, monkeypatch, sub):
+    """Every loss kernel variant (block shape) and target sort order gives the
+    identical trajectory, equal to the oracle's: the sums are order free."""
+    from voromesh_gb300 import synth
+
+    monkeypatch.setenv("VM_TARGET_SUB", sub)
+    gen = synth.uniform(5, 1, 2048)
+    tgt = synth.circle(5, 2, 60000, 0.7, 2e-3)
+    opt, ref = _pair(vm, orc, gen, tgt, 0.04, 16, 0, 1.0)
+    ref.step(6)
+    g, m, v = ref.generators()
+    _, count = opt.LossVariant()
+    for variant in range(count):
+        opt.SetLossVariant(variant)
+        opt.SetGenerators(gen, len(gen), 1, 2.0)
+        opt.Step(6)
+        assert np.array_equal(opt.Generators(), g), f"variant {variant}"
