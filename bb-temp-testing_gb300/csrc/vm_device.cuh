@@ -53,7 +53,7 @@ __device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) 
 
 // round-half-even(v * 2^e) as int64, saturating at +-2^62, NaN -> 0; integer
 // operations only (64-bit float->int conversions run on the narrow FP64 pipe).
-__device__ __forceinline__ long long fx_from_float(float v, int e)
+static __device__ __noinline__ long long fx_from_float_any(float v, int e)
 {
     unsigned u = __float_as_uint(v);
     int ex = (int)((u >> 23) & 0xFFu);
@@ -81,6 +81,20 @@ __device__ __forceinline__ long long fx_from_float(float v, int e)
         mag = q;
     }
     return (u >> 31) ? -mag : mag;
+}
+
+// The same with the common case inline: a normal v whose scaled value is an
+// integer below 2^62 (a plain shift of the significand, no rounding).
+__device__ __forceinline__ long long fx_from_float(float v, int e)
+{
+    unsigned u = __float_as_uint(v);
+    int ex = (int)((u >> 23) & 0xFFu);
+    int k = ex - 150 + e;
+    if ((unsigned)(ex - 1) < 254u && (unsigned)k <= 38u) {
+        long long mag = (long long)((u & 0x7FFFFFu) | 0x800000u) << k;
+        return (u >> 31) ? -mag : mag;
+    }
+    return fx_from_float_any(v, e);
 }
 
 __device__ __forceinline__ float fx_to_float(long long v, int e) { return __ll2float_rn(v) * pow2f(-e); }

@@ -435,8 +435,9 @@ __device__ __forceinline__ int loss_staged(const VmFit &F, WarpStage &W, bool ta
         }
     };
     for (int q = 0; q < n1; ++q) consider(W.near[q]);
-    // 0.1% slack covers every float rounding in this chain of bounds
-    float sqD0 = sqrtf(d0);
+    // 0.1% slack covers every float rounding in this chain of bounds; sqD0 is
+    // within 4 ulp of sqrt(d0) (only bounds use it)
+    float sqD0 = d0 > 0.0f ? d0 * rsqrtf(d0) : 0.0f;
     float T = best < FLT_MAX ? 1.001f * (sqD0 + 2.0f * (best + bestEps)) : FLT_MAX;
     T = T < FLT_MAX ? T * T + 1e-30f : FLT_MAX;
     if (!take) T = 0.0f;
