@@ -116,6 +116,9 @@ __device__ __forceinline__ void grid_tile_apply(const VmPointSet &S, int tile)
     int v[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) v[k] = base + k < cells ? S.counts[base + k] : 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (base + k < cells) S.counts[base + k] = 0; // zero again for the next build
     int total;
     int excl = block_scan8(v, ws, total);
 #pragma unroll
@@ -125,8 +128,8 @@ __device__ __forceinline__ void grid_tile_apply(const VmPointSet &S, int tile)
     if (tile == tiles - 1 && threadIdx.x == 0) S.start[cells] = offset + total;
 }
 
-// Cell-sorted copy of point i; the last writer of each cell sorts the cell's
-// run by point index (canonical order) and the counts return to zero.
+// Cell-sorted copy of point i (its rank within the cell is the arrival order
+// of the binning atomics).
 __device__ __forceinline__ void grid_scatter_one(const VmPointSet &S, int i)
 {
     if (i >= S.n) return;
@@ -135,27 +138,31 @@ __device__ __forceinline__ void grid_scatter_one(const VmPointSet &S, int i)
     int s = S.start[c] + S.rank[i];
     S.outIdx[s] = i;
     S.outPos[s] = S.pts[i];
-    __threadfence();
-    int left = atomicSub(&S.counts[c], 1);
-    if (S.canonical && left == 1) {
-        // last writer of cell c: all writes to its run are visible after the fence
-        __threadfence();
+}
+
+// Canonical order of the runs of one scan tile's cells: ascending point index
+// (insertion sort; a run holds a few points). 256-thread block.
+__device__ __forceinline__ void grid_canonical_tile(const VmPointSet &S, int tile)
+{
+    int cells = grid_keys(S);
+#pragma unroll 1
+    for (int k = 0; k < kScanTile / 256; ++k) {
+        int c = tile * kScanTile + k * 256 + threadIdx.x;
+        if (c >= cells) return;
         int b = S.start[c], e = S.start[c + 1];
-        if (e - b > 1) {
-            for (int a = b + 1; a < e; ++a) {
-                int id = __ldcg(&S.outIdx[a]);
-                float2 ps = __ldcg(&S.outPos[a]);
-                int k = a - 1;
-                while (k >= b) {
-                    int ik = __ldcg(&S.outIdx[k]);
-                    if (ik <= id) break;
-                    S.outIdx[k + 1] = ik;
-                    S.outPos[k + 1] = __ldcg(&S.outPos[k]);
-                    --k;
-                }
-                S.outIdx[k + 1] = id;
-                S.outPos[k + 1] = ps;
+        for (int a = b + 1; a < e; ++a) {
+            int id = S.outIdx[a];
+            float2 ps = S.outPos[a];
+            int q = a - 1;
+            while (q >= b) {
+                int iq = S.outIdx[q];
+                if (iq <= id) break;
+                S.outIdx[q + 1] = iq;
+                S.outPos[q + 1] = S.outPos[q];
+                --q;
             }
+            S.outIdx[q + 1] = id;
+            S.outPos[q + 1] = ps;
         }
     }
 }

@@ -10,11 +10,15 @@ cudaError_t vm_launch_bin(const VmPointSet *sets, const int *prefix, int nSets, 
 cudaError_t vm_launch_scan(const VmPointSet *sets, const int *tilePrefix, int nSets, int totalTiles, cudaStream_t s);
 cudaError_t vm_launch_scatter(const VmPointSet *sets, const int *prefix, int nSets, int totalBlocks,
                               const VmFit *publish, cudaStream_t s);
+// Sorts each cell's run by point index (sets with canonical = 0 are skipped);
+// one block per scan tile, the same tile prefix as vm_launch_scan.
+cudaError_t vm_launch_canonical(const VmPointSet *sets, const int *tilePrefix, int nSets, int totalTiles,
+                                cudaStream_t s);
 // The loss pass is two launches: the block-certified fast path over all
 // targets, then the exact ring search over the targets it deferred to the
 // queue (created by vm_queue_init; items hold (fit, target) int2 pairs).
-// `variant` picks block size, occupancy target and gradient aggregation; its
-// block size is also the number of targets per tile the prefix table counts.
+// `variant` picks block size and occupancy target; its block size is also the
+// number of targets per tile the prefix table counts.
 cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode, int maxR,
                            int gridBlocks, int variant, void *queue, cudaStream_t s);
 int vm_loss_variants();

@@ -242,6 +242,7 @@ int enqueue_build_grid(vm_optimizer *h)
     if ((e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "scan");
     if ((e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, nullptr, h->stream)))
         return cuda_fail(e, "scatter");
+    if ((e = vm_launch_canonical(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "canonical");
     return VM_OK;
 }
 
@@ -266,6 +267,7 @@ int enqueue_step(vm_optimizer *h)
     if ((e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "scan");
     if ((e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, h->dFit.p, h->stream)))
         return cuda_fail(e, "scatter");
+    if ((e = vm_launch_canonical(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "canonical");
     return VM_OK;
 }
 
@@ -691,6 +693,7 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
             (e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream)) ||
             (e = cudaEventRecord(ev[3], h->stream)) ||
             (e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, h->dFit.p, h->stream)) ||
+            (e = vm_launch_canonical(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream)) ||
             (e = cudaEventRecord(ev[4], h->stream)))
             return cuda_fail(e, "timed step");
     }

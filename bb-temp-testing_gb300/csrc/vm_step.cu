@@ -3,8 +3,8 @@
 //   k_bin          cell key + atomic count per point        (reference binKernel, voro_optimizer.cu:168-177)
 //   k_scan_tiles   per-tile sums of the cell counts          (reference cub ExclusiveSum, :697)
 //   k_scan_apply   exclusive scan -> cell start
-//   k_scatter      cell-sorted copy; the last writer of each cell sorts its run by
-//                  slot index, so the ordering is canonical (reference scatterKernel :179-187)
+//   k_scatter      cell-sorted copy (reference scatterKernel :179-187)
+//   k_canonical    each cell's run sorted by slot index, so the order is canonical
 //   (k_loss        VoroLoss + analytic gradient per target, vm_loss.cu)
 //   k_adam_bin     Adam + MultiStepLR + clamp, fused with the next step's binning
 //                  (reference adamKernel :271-301 + binKernel)
@@ -12,7 +12,7 @@
 //   k_knn          exact kNN query operator (reference knn<K>, :130-163)
 //
 // One step of a set of fits is: k_loss -> k_adam_bin -> k_scan_tiles ->
-// k_scan_apply -> k_scatter(publish). The grid is therefore always built for
+// k_scan_apply -> k_scatter(publish) -> k_canonical. The grid is therefore always built for
 // the current generators between steps, as the reference rebuilds it at the
 // start of each step.
 #include "vm_device.cuh"
@@ -44,6 +44,13 @@ __global__ void __launch_bounds__(256) k_scan_apply(const VmPointSet *__restrict
 {
     int f = find_fit(prefix, nSets, blockIdx.x);
     grid_tile_apply(sets[f], blockIdx.x - prefix[f]);
+}
+
+__global__ void __launch_bounds__(256) k_canonical(const VmPointSet *__restrict__ sets,
+                                                   const int *__restrict__ prefix, int nSets)
+{
+    int f = find_fit(prefix, nSets, blockIdx.x);
+    if (sets[f].canonical) grid_canonical_tile(sets[f], blockIdx.x - prefix[f]);
 }
 
 __global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ sets, const int *__restrict__ prefix,
@@ -196,6 +203,14 @@ cudaError_t vm_launch_scan(const VmPointSet *sets, const int *tilePrefix, int nS
     if (totalTiles <= 0) return cudaSuccess;
     k_scan_tiles<<<totalTiles, 256, 0, s>>>(sets, tilePrefix, nSets);
     k_scan_apply<<<totalTiles, 256, 0, s>>>(sets, tilePrefix, nSets);
+    return cudaGetLastError();
+}
+
+cudaError_t vm_launch_canonical(const VmPointSet *sets, const int *tilePrefix, int nSets, int totalTiles,
+                                cudaStream_t s)
+{
+    if (totalTiles <= 0) return cudaSuccess;
+    k_canonical<<<totalTiles, 256, 0, s>>>(sets, tilePrefix, nSets);
     return cudaGetLastError();
 }
 
