@@ -200,6 +200,35 @@ __device__ __forceinline__ int find_fit(const int *prefix, int nFits, int b)
     return lo;
 }
 
+// base^t in double by exponentiation by squaring, rounded to float once: a
+// deterministic stand-in for powf in the Adam bias corrections.
+__device__ __forceinline__ float pow_det(float base, int t)
+{
+    double r = 1.0, x = (double)base;
+    unsigned e = t < 0 ? 0u : (unsigned)t;
+    while (e) {
+        if (e & 1u) r = __dmul_rn(r, x);
+        x = __dmul_rn(x, x);
+        e >>= 1;
+    }
+    return __double2float_rn(r);
+}
+
+// The learning rate (MultiStepLR) and bias corrections of fit F's next step
+// t = iter + 1 (reference adamKernel, voro_optimizer.cu:271-301), written to
+// its state for the Adam kernel.
+__device__ __forceinline__ void adam_schedule(const VmFit &F)
+{
+    VmState *st = F.state;
+    int t = st->iter + 1;
+    float lr = F.lr;
+    for (int k = 0; k < 4; ++k)
+        if (t - 1 >= F.milestones[k]) lr *= F.gamma;
+    st->schedLr = lr;
+    st->schedBc1 = 1.0f - pow_det(F.beta1, t);
+    st->schedBc2 = 1.0f - pow_det(F.beta2, t);
+}
+
 // Targets the loss kernel's block certificates could not settle are deferred
 // to this queue and resolved by k_loss_exact in dense warps, so one hard
 // target does not stall the 31 other lanes of its warp on the long ring

@@ -140,30 +140,25 @@ __device__ __forceinline__ void grid_scatter_one(const VmPointSet &S, int i)
     S.outPos[s] = S.pts[i];
 }
 
-// Canonical order of the runs of one scan tile's cells: ascending point index
-// (insertion sort; a run holds a few points). 256-thread block.
-__device__ __forceinline__ void grid_canonical_tile(const VmPointSet &S, int tile)
+// Canonical order of cell c's run: ascending point index (insertion sort; a
+// run holds a few points).
+__device__ __forceinline__ void grid_canonical_one(const VmPointSet &S, int c)
 {
-    int cells = grid_keys(S);
-#pragma unroll 1
-    for (int k = 0; k < kScanTile / 256; ++k) {
-        int c = tile * kScanTile + k * 256 + threadIdx.x;
-        if (c >= cells) return;
-        int b = S.start[c], e = S.start[c + 1];
-        for (int a = b + 1; a < e; ++a) {
-            int id = S.outIdx[a];
-            float2 ps = S.outPos[a];
-            int q = a - 1;
-            while (q >= b) {
-                int iq = S.outIdx[q];
-                if (iq <= id) break;
-                S.outIdx[q + 1] = iq;
-                S.outPos[q + 1] = S.outPos[q];
-                --q;
-            }
-            S.outIdx[q + 1] = id;
-            S.outPos[q + 1] = ps;
+    if (c >= grid_keys(S)) return;
+    int b = S.start[c], e = S.start[c + 1];
+    for (int a = b + 1; a < e; ++a) {
+        int id = S.outIdx[a];
+        float2 ps = S.outPos[a];
+        int q = a - 1;
+        while (q >= b) {
+            int iq = S.outIdx[q];
+            if (iq <= id) break;
+            S.outIdx[q + 1] = iq;
+            S.outPos[q + 1] = S.outPos[q];
+            --q;
         }
+        S.outIdx[q + 1] = id;
+        S.outPos[q + 1] = ps;
     }
 }
 

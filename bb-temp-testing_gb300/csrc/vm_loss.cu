@@ -707,9 +707,14 @@ __global__ void __launch_bounds__(THREADS, MINB)
 }
 
 // The deferred targets: exact ring search, one target per thread, with the
-// loss, count and gradient added straight into the fit's accumulators.
-__global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fits, int mode, SlowQueue *queue)
+// loss, count and gradient added straight into the fit's accumulators. In a
+// step pass it also writes each fit's Adam schedule for the step.
+__global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fits, int nFits, int mode,
+                                                    SlowQueue *queue)
 {
+    if (mode == 0)
+        for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nFits; f += gridDim.x * blockDim.x)
+            if (fits[f].active) adam_schedule(fits[f]); // for the Adam kernel that follows
     int n = min(queue->count, queue->capacity);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
         int2 it = queue->items[q];
@@ -788,7 +793,7 @@ cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, 
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_loss_exact<<<sms * 2, 128, 0, s>>>(fits, mode, q);
+    k_loss_exact<<<sms * 2, 128, 0, s>>>(fits, nFits, mode, q);
     return cudaGetLastError();
 }
 

@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(256) k_na_bin(VmPointSet S) { vmk::grid_bin_on
 __global__ void __launch_bounds__(256) k_na_tile_sum(VmPointSet S) { vmk::grid_tile_sum(S, blockIdx.x); }
 __global__ void __launch_bounds__(256) k_na_tile_apply(VmPointSet S) { vmk::grid_tile_apply(S, blockIdx.x); }
 __global__ void __launch_bounds__(256) k_na_scatter(VmPointSet S) { vmk::grid_scatter_one(S, blockIdx.x * blockDim.x + threadIdx.x); }
-__global__ void __launch_bounds__(256) k_na_canonical(VmPointSet S) { vmk::grid_canonical_tile(S, blockIdx.x); }
+__global__ void __launch_bounds__(256) k_na_canonical(VmPointSet S) { vmk::grid_canonical_one(S, blockIdx.x * blockDim.x + threadIdx.x); }
 
 constexpr int kMaxDevices = 64;
 char *g_scratchAddr[kMaxDevices]; // device address of g_noallocScratch, per device
@@ -105,7 +105,7 @@ extern "C" int vm_build_grid_noalloc(const float *generators, int n, int gridW, 
     k_na_tile_sum<<<tiles, 256, 0, s>>>(S);
     k_na_tile_apply<<<tiles, 256, 0, s>>>(S);
     if (blocks) k_na_scatter<<<blocks, 256, 0, s>>>(S);
-    k_na_canonical<<<tiles, 256, 0, s>>>(S);
+    k_na_canonical<<<(cells + 255) / 256, 256, 0, s>>>(S);
     if ((e = cudaGetLastError()) != cudaSuccess) return vmh::cuda_fail(e, "vm_build_grid_noalloc launch");
     return VM_OK;
 }

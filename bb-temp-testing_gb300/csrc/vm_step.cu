@@ -6,8 +6,9 @@
 //   k_scatter      cell-sorted copy (reference scatterKernel :179-187)
 //   k_canonical    each cell's run sorted by slot index, so the order is canonical
 //   (k_loss        VoroLoss + analytic gradient per target, vm_loss.cu)
-//   k_adam_bin     Adam + MultiStepLR + clamp, fused with the next step's binning
-//                  (reference adamKernel :271-301 + binKernel)
+//   k_adam_bin     Adam + clamp, fused with the next step's binning (reference
+//                  adamKernel :271-301 + binKernel); its lr and bias corrections
+//                  come from adam_schedule in the loss pass
 //   k_finalize     publish a loss-only pass (EvaluateLoss, :746-761)
 //   k_knn          exact kNN query operator (reference knn<K>, :130-163)
 //
@@ -49,8 +50,10 @@ __global__ void __launch_bounds__(256) k_scan_apply(const VmPointSet *__restrict
 __global__ void __launch_bounds__(256) k_canonical(const VmPointSet *__restrict__ sets,
                                                    const int *__restrict__ prefix, int nSets)
 {
-    int f = find_fit(prefix, nSets, blockIdx.x);
-    if (sets[f].canonical) grid_canonical_tile(sets[f], blockIdx.x - prefix[f]);
+    // kScanTile / 256 blocks per scan tile, one thread per cell
+    constexpr int kPer = kScanTile / 256;
+    int f = find_fit(prefix, nSets, blockIdx.x / kPer);
+    if (sets[f].canonical) grid_canonical_one(sets[f], (blockIdx.x - prefix[f] * kPer) * 256 + threadIdx.x);
 }
 
 __global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ sets, const int *__restrict__ prefix,
@@ -89,47 +92,31 @@ __global__ void k_finalize(const VmFit *__restrict__ fits, int nFits, SlowQueue 
 // ---------------------------------------------------------------------------
 // Adam (fused with the next grid's binning)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float pow_det(float base, int t)
-{
-    double r = 1.0, x = (double)base;
-    unsigned e = t < 0 ? 0u : (unsigned)t;
-    while (e) {
-        if (e & 1u) r = __dmul_rn(r, x);
-        x = __dmul_rn(x, x);
-        e >>= 1;
-    }
-    return __double2float_rn(r);
-}
-
 __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits, const int *__restrict__ prefix,
                                                   int nFits, SlowQueue *queue)
 {
-    __shared__ float sLr, sBc1, sBc2, sScale;
     if (blockIdx.x == 0 && threadIdx.x == 0) queue->count = 0;
     int f = find_fit(prefix, nFits, blockIdx.x);
     const VmFit &F = fits[f];
     if (!F.active) return;
-    if (threadIdx.x == 0) {
-        int t = F.state->iter + 1;
-        float lr = F.lr;
-        for (int k = 0; k < 4; ++k)
-            if (t - 1 >= F.milestones[k]) lr *= F.gamma;
-        sLr = lr;
-        sBc1 = 1.0f - pow_det(F.beta1, t);
-        sBc2 = 1.0f - pow_det(F.beta2, t);
-        int count = F.state->accCount;
-        sScale = 1.0f / (float)(count > 1 ? count : 1);
-    }
-    __syncthreads();
     int i = (blockIdx.x - prefix[f]) * blockDim.x + threadIdx.x;
     if (i >= F.nSlots) return;
+    // lr and bias corrections of this step (adam_schedule, run by the loss pass)
+    const VmState *st = F.state;
+    float lr = st->schedLr, bc1 = st->schedBc1, bc2 = st->schedBc2;
+    int count = st->accCount;
+    float scale = 1.0f / (float)(count > 1 ? count : 1);
     longlong2 gq = reinterpret_cast<const longlong2 *>(F.gradX)[i];
     if (gq.x | gq.y) reinterpret_cast<longlong2 *>(F.gradX)[i] = make_longlong2(0, 0);
     float2 p = F.gen[i];
-    int sx = i % F.slotsW, sy = i / F.slotsW;
-    if (p.x >= 0.0f && sx >= F.cx0 && sx < F.cx1 && sy >= F.cy0 && sy < F.cy1) {
-        float grx = sScale * fx_to_float(gq.x, F.gradExp);
-        float gry = sScale * fx_to_float(gq.y, F.gradExp);
+    bool inRegion = true;
+    if (F.cx0 != 0 || F.cy0 != 0 || F.cx1 != F.slotsW || F.cy1 != F.slotsH) {
+        int sx = i % F.slotsW, sy = i / F.slotsW;
+        inRegion = sx >= F.cx0 && sx < F.cx1 && sy >= F.cy0 && sy < F.cy1;
+    }
+    if (p.x >= 0.0f && inRegion) {
+        float grx = scale * fx_to_float(gq.x, F.gradExp);
+        float gry = scale * fx_to_float(gq.y, F.gradExp);
         float2 m = F.m[i], v = F.v[i];
         float b1 = F.beta1, b2 = F.beta2;
         float mx = b1 * m.x + (1.0f - b1) * grx;
@@ -138,7 +125,7 @@ __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits
         float vy = b2 * v.y + (1.0f - b2) * (gry * gry);
         F.m[i] = make_float2(mx, my);
         F.v[i] = make_float2(vx, vy);
-        float lr = sLr, bc1 = sBc1, bc2 = sBc2, eps = F.eps;
+        float eps = F.eps;
         p.x -= lr * (mx / bc1) / (sqrtf(vx / bc2) + eps);
         p.y -= lr * (my / bc1) / (sqrtf(vy / bc2) + eps);
         p.x = fminf(fmaxf(p.x, 0.0f), F.width);
@@ -210,7 +197,7 @@ cudaError_t vm_launch_canonical(const VmPointSet *sets, const int *tilePrefix, i
                                 cudaStream_t s)
 {
     if (totalTiles <= 0) return cudaSuccess;
-    k_canonical<<<totalTiles, 256, 0, s>>>(sets, tilePrefix, nSets);
+    k_canonical<<<totalTiles * (kScanTile / 256), 256, 0, s>>>(sets, tilePrefix, nSets);
     return cudaGetLastError();
 }
 

@@ -28,7 +28,8 @@ struct VmState {
     int accCount;    // used-target counter of the running pass
     int slowTotal;   // targets that needed the exact ring search (cumulative)
     int errors;      // error bits raised by kernels (see VM_KERR_*)
-    int pad[19];
+    float schedLr, schedBc1, schedBc2; // this step's learning rate and bias corrections
+    int pad[16];
 };
 
 enum : int {
