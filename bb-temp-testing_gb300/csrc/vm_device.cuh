@@ -31,7 +31,7 @@ __device__ __forceinline__ bool key_less(float dd, int id, float D, int I)
 }
 
 // Stateless RNG (reference voro_optimizer.cu:69-78, poisson_disk.cu:47-58).
-__device__ __forceinline__ unsigned pcg_hash(unsigned v)
+__host__ __device__ __forceinline__ unsigned pcg_hash(unsigned v)
 {
     unsigned state = v * 747796405u + 2891336453u;
     unsigned word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;

@@ -11,35 +11,51 @@
 // the inputs and the sequence of regions resampled.
 //
 // Each phase is one launch over the phase cells of the region.
+#include <algorithm>
+
 #include "vm_device.cuh"
 #include "vm_kernels.h"
 
 namespace vmk {
 
-__device__ __forceinline__ float prand01(unsigned cell, unsigned round, unsigned seed, unsigned stream)
+// Dart coordinate stream `stream` of a round: the per-round part of the hash
+// chain, computed once per launch on the host.
+__host__ __device__ __forceinline__ unsigned round_key(unsigned round, unsigned seed, unsigned stream)
 {
-    unsigned h = pcg_hash(cell ^ pcg_hash(round * 2654435761u ^ pcg_hash(seed + stream * 0x9E3779B9u)));
+    return pcg_hash(round * 2654435761u ^ pcg_hash(seed + stream * 0x9E3779B9u));
+}
+
+// uniform [0,1) of (cell, round, seed, stream): pcg_hash(cell ^ round_key)
+__device__ __forceinline__ float prand01(unsigned cell, unsigned key)
+{
+    unsigned h = pcg_hash(cell ^ key);
     return (float)(h & 0x00FFFFFFu) * (1.0f / 16777216.0f);
 }
 
+// The 5x5 block around a cell without the cell itself, by distance.
+__constant__ signed char kRingDx[24] = {0, -1, 1, 0, -1, 1, -1, 1, 0, -2, 2, 0, -1, 1, -2, 2, -2, 2, -1, 1, -2, 2, -2, 2};
+__constant__ signed char kRingDy[24] = {-1, 0, 0, 1, -1, -1, 1, 1, -2, 0, 0, 2, -2, -2, -1, -1, 1, 1, 2, 2, -2, -2, 2, 2};
+
 // One dart for cell (cx, cy) (reference dartPhaseKernel :84-106).
-__device__ __forceinline__ void dart(float2 *grid, const PdParams &p, int cx, int cy, unsigned round)
+__device__ __forceinline__ void dart(float2 *grid, const PdParams &p, int cx, int cy, unsigned keyX, unsigned keyY)
 {
     int cellId = cy * p.gridW + cx;
     if (grid[cellId].x >= 0.0f) return;
-    float x = ((float)cx + prand01((unsigned)cellId, round, p.seed, 0u)) * p.cellSize;
-    float y = ((float)cy + prand01((unsigned)cellId, round, p.seed, 1u)) * p.cellSize;
+    float x = ((float)cx + prand01((unsigned)cellId, keyX)) * p.cellSize;
+    float y = ((float)cy + prand01((unsigned)cellId, keyY)) * p.cellSize;
     if (x >= p.width || y >= p.height) return;
     float r2 = p.radius * p.radius;
-    int x0 = max(cx - 2, 0), x1 = min(cx + 2, p.gridW - 1);
-    int y0 = max(cy - 2, 0), y1 = min(cy + 2, p.gridH - 1);
-    for (int ny = y0; ny <= y1; ++ny)
-        for (int nx = x0; nx <= x1; ++nx) {
-            float2 q = grid[ny * p.gridW + nx];
-            if (q.x < 0.0f) continue;
-            float dx = q.x - x, dy = q.y - y;
-            if (dx * dx + dy * dy < r2) return;
-        }
+    // the 24 neighbours nearest first, so most rejected darts stop early (the
+    // dart lands only if none conflicts, whatever the order)
+#pragma unroll 4
+    for (int k = 0; k < 24; ++k) {
+        int nx = cx + kRingDx[k], ny = cy + kRingDy[k];
+        if (nx < 0 || nx >= p.gridW || ny < 0 || ny >= p.gridH) continue;
+        float2 q = grid[ny * p.gridW + nx];
+        if (q.x < 0.0f) continue;
+        float dx = q.x - x, dy = q.y - y;
+        if (dx * dx + dy * dy < r2) return;
+    }
     grid[cellId] = make_float2(x, y);
 }
 
@@ -53,16 +69,16 @@ __global__ void __launch_bounds__(256) k_clear(float2 *grid, int gridW, int x0, 
     }
 }
 
-// One phase (px, py) of one round, one thread per phase cell.
+// One phase (px, py) of one round, one thread per phase cell: x across the
+// threads of a block row, phase rows over blockIdx.y.
 __global__ void __launch_bounds__(256) k_phase(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int px,
-                                               int py, unsigned round)
+                                               int py, unsigned keyX, unsigned keyY)
 {
     int tw = (x1 - x0 - px + 2) / 3, th = (y1 - y0 - py + 2) / 3;
-    long long n = (long long)tw * th;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        int tx = (int)(t % tw), ty = (int)(t / tw);
-        dart(grid, p, x0 + 3 * tx + px, y0 + 3 * ty + py, round);
-    }
+    int tx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tx >= tw) return;
+    for (int ty = blockIdx.y; ty < th; ty += gridDim.y)
+        dart(grid, p, x0 + 3 * tx + px, y0 + 3 * ty + py, keyX, keyY);
 }
 
 } // namespace vmk
@@ -78,12 +94,12 @@ cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1,
     int cb = (int)((cells + 255) / 256);
     if (cb > 65535) cb = 65535;
     k_clear<<<cb, 256, 0, s>>>(grid, p.gridW, x0, y0, x1, y1);
-    long long phaseCells = ((long long)(rw + 2) / 3) * ((rh + 2) / 3);
-    int pb = (int)((phaseCells + 255) / 256);
-    if (pb > 65535) pb = 65535;
-    for (int round = 0; round < trials; ++round)
+    dim3 pb((unsigned)((rw + 2) / 3 + 255) / 256, (unsigned)std::min((rh + 2) / 3, 65535));
+    for (int round = 0; round < trials; ++round) {
+        unsigned r = roundBase + (unsigned)round;
+        unsigned kx = round_key(r, p.seed, 0u), ky = round_key(r, p.seed, 1u);
         for (int py = 0; py < 3; ++py)
-            for (int px = 0; px < 3; ++px)
-                k_phase<<<pb, 256, 0, s>>>(grid, p, x0, y0, x1, y1, px, py, roundBase + (unsigned)round);
+            for (int px = 0; px < 3; ++px) k_phase<<<pb, 256, 0, s>>>(grid, p, x0, y0, x1, y1, px, py, kx, ky);
+    }
     return cudaGetLastError();
 }
