@@ -132,7 +132,8 @@ int single_set_build(vmb_batch *b, const VmPointSet &S, int emptyIsNegative, int
     VmPointSet T = S;
     T.canonical = canonical;
     int blocks = (T.n + 255) / 256;
-    int tiles = (T.gridW * T.gridH + kScanTile - 1) / kScanTile;
+    long long keys = (long long)T.gridW * T.gridH << (2 * T.sub);
+    int tiles = (int)((keys + kScanTile - 1) / kScanTile);
     int pre[4] = {0, blocks, 0, tiles};
     cudaError_t e;
     if ((e = cudaMemcpyAsync(b->dOneSet.p, &T, sizeof(T), cudaMemcpyHostToDevice, b->stream)) ||
@@ -397,17 +398,51 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
         release_fit(b, f);
         return cuda_fail(e, "vmb_add_fit upload");
     }
+    // targets sorted by (cell, 4x4 sub-cell) with temporary key arrays from the
+    // arena; by cell alone, in the grid's arrays, if those do not fit
+    int sub = 2;
+    while (sub > 0 && ((long long)f.cells << (2 * sub)) > (1LL << 27)) --sub;
+    long long keys = (long long)f.cells << (2 * sub);
+    size_t tmpSizes[3] = {4 * (size_t)(keys + 1), 4 * (size_t)(keys + 1),
+                          4 * (size_t)((keys + kScanTile - 1) / kScanTile + 1)};
+    size_t tmpOff[3];
+    int nTmp = 0;
+    if (sub > 0)
+        for (; nTmp < 3; ++nTmp)
+            if (!b->arena.alloc(tmpSizes[nTmp], &tmpOff[nTmp])) break;
+    auto releaseTmp = [&]() {
+        for (int k = 0; k < nTmp; ++k) b->arena.release(tmpOff[k], tmpSizes[k]);
+        nTmp = 0;
+    };
+    int *liveAt = D.start + f.cells;
+    if (nTmp == 3) {
+        f.tset.sub = sub;
+        f.tset.counts = reinterpret_cast<int *>(b->arena.base + tmpOff[0]);
+        f.tset.start = reinterpret_cast<int *>(b->arena.base + tmpOff[1]);
+        f.tset.tileSums = reinterpret_cast<int *>(b->arena.base + tmpOff[2]);
+        liveAt = f.tset.start + keys;
+        if ((e = cudaMemsetAsync(f.tset.counts, 0, tmpSizes[0], b->stream))) {
+            releaseTmp();
+            release_fit(b, f);
+            return cuda_fail(e, "vmb_add_fit sort keys");
+        }
+    } else {
+        releaseTmp();
+    }
     int rc;
-    if ((rc = single_set_build(b, f.tset, 0, 0))) { // targets sorted by cell
+    if ((rc = single_set_build(b, f.tset, 0, 0))) {
+        releaseTmp();
         release_fit(b, f);
         return rc;
     }
     int live = 0;
-    if ((e = cudaMemcpyAsync(&live, D.start + f.cells, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
+    if ((e = cudaMemcpyAsync(&live, liveAt, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
         (e = cudaStreamSynchronize(b->stream))) {
+        releaseTmp();
         release_fit(b, f);
         return cuda_fail(e, "vmb_add_fit live targets");
     }
+    releaseTmp();
     f.liveTargets = live;
     D.nTargets = live;
     if ((rc = single_set_build(b, f.sites, 1, 1))) { // the grid of the initial generators
@@ -522,6 +557,26 @@ int vmb_memory(vmb_batch *b, size_t *freeBytes, size_t *totalBytes, int *liveFit
 // ---------------------------------------------------------------------------
 // serving loop
 // ---------------------------------------------------------------------------
+} // extern "C"
+
+namespace {
+
+// Every fit's loss per target from its last step's loss pass.
+int step_losses(vmb_batch *b, float *losses)
+{
+    int rc;
+    if ((rc = read_states(b))) return rc;
+    for (int id = 0; id < (int)b->fits.size(); ++id) {
+        const VmState &s = b->hostStates[id];
+        losses[id] = s.count > 0 ? s.loss / (float)s.count : 0.0f;
+    }
+    return VM_OK;
+}
+
+} // namespace
+
+extern "C" {
+
 int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result *res)
 {
     if (n < 0 || (n && (!reqs || !res)) || !cfg || cfg->stepsPerRound < 1 || cfg->maxLive < 1)
@@ -578,8 +633,14 @@ int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result 
             }
             continue;
         }
-        // step all live fits together, then judge each on its full-target loss
-        if ((rc = vmb_step(b, cfg->stepsPerRound, nullptr)) || (rc = vmb_evaluate(b, losses.data()))) {
+        // step all live fits together, then judge each on its full-target loss:
+        // the loss pass of the round's last step when every target counts every
+        // step (sampleFraction 1), else a separate full-target evaluation
+        bool evaluate = false;
+        for (int id = 0; id < (int)liveReq.size(); ++id)
+            if (liveReq[id] >= 0 && reqs[liveReq[id]].fit.params.sampleFraction < 1.0f) evaluate = true;
+        if ((rc = vmb_step(b, cfg->stepsPerRound, nullptr)) ||
+            (rc = evaluate ? vmb_evaluate(b, losses.data()) : step_losses(b, losses.data()))) {
             vmb_destroy(b);
             return rc;
         }

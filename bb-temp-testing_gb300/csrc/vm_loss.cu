@@ -646,7 +646,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 }
                 if (r < 0) {
                     int q = atomicAdd(&queue->count, 1);
-                    queue->items[q] = make_int2(f, local); // capacity >= live targets
+                    if (q < queue->capacity) queue->items[q] = make_int2(f, local); // capacity >= live targets
+                    else atomicOr(&F.state->errors, VM_KERR_CAPACITY);
                     r = 0;
                     deferred = true;
                     aSlow += 1;

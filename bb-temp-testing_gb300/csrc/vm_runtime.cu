@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -141,6 +142,7 @@ struct vm_optimizer {
     int lossTile = 256;    // targets per loss tile (= its block size)
     int lossVariant = 3;   // loss kernel variant in use
     int lossForced = -1;   // variant chosen by the caller (vm_set_loss_variant), -1 = automatic
+    bool tunePending = false; // the autotuner still has to pick the variant
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -219,8 +221,16 @@ void drop_graph(vm_optimizer *h)
     h->graph = nullptr;
 }
 
-// Loss kernel variant: the caller's choice, else VM_LOSS_VARIANT, else 64-thread
-// tiles for small fits (more blocks in flight) and 256-thread tiles otherwise.
+void set_loss_variant(vm_optimizer *h, int v)
+{
+    h->lossVariant = v;
+    h->lossTile = vm_loss_variant_threads(v);
+    h->lossGrid = vm_loss_occupancy_blocks(v);
+}
+
+// Loss kernel variant: the caller's choice, else VM_LOSS_VARIANT, else the
+// autotuner's choice for this fit size (made at the first step; until then
+// 64-thread tiles for small fits and 256-thread tiles otherwise).
 void choose_loss_variant(vm_optimizer *h, int sms)
 {
     int v = h->lossForced;
@@ -228,10 +238,79 @@ void choose_loss_variant(vm_optimizer *h, int sms)
         const char *env = std::getenv("VM_LOSS_VARIANT");
         if (env && *env) v = std::atoi(env);
     }
-    if (v < 0 || v >= vm_loss_variants()) v = h->liveTargets < 256 * 4 * sms ? 5 : 1;
-    h->lossVariant = v;
-    h->lossTile = vm_loss_variant_threads(v);
-    h->lossGrid = vm_loss_occupancy_blocks(v);
+    h->tunePending = v < 0 || v >= vm_loss_variants();
+    if (h->tunePending) v = h->liveTargets < 256 * 4 * sms ? 5 : 1;
+    set_loss_variant(h, v);
+}
+
+// The autotuner: per power-of-two bucket of live targets, the loss variant
+// with the shortest measured pass, kept for the process.
+std::mutex g_tuneMu;
+int g_tuned[64];
+bool g_tunedInit = false;
+
+int tune_bucket(int live)
+{
+    int b = 0;
+    while (b < 62 && (2LL << b) <= live) ++b;
+    return b;
+}
+
+int read_state(vm_optimizer *h, VmState &st);
+
+// Times every variant on this fit (3 loss passes each, after one untimed
+// pass, in two sweeps) and keeps the fastest. The passes leave the generators and moments
+// alone; the gradient accumulators and the state are restored afterwards.
+int autotune_loss_variant(vm_optimizer *h)
+{
+    h->tunePending = false;
+    int bucket = tune_bucket(h->liveTargets);
+    {
+        std::lock_guard<std::mutex> lk(g_tuneMu);
+        if (!g_tunedInit) {
+            for (int &t : g_tuned) t = -1;
+            g_tunedInit = true;
+        }
+        if (g_tuned[bucket] >= 0) {
+            set_loss_variant(h, g_tuned[bucket]);
+            return upload_tables(h);
+        }
+    }
+    VmState saved;
+    int rc;
+    if ((rc = read_state(h, saved))) return rc;
+    int nv = vm_loss_variants();
+    std::vector<float> score(nv, 1e30f);
+    cudaError_t e;
+    for (int round = 0; round < 2; ++round) // the better of two sweeps, against noise and warm-up
+        for (int v = 0; v < nv; ++v) {
+            set_loss_variant(h, v);
+            if ((rc = upload_tables(h))) return rc;
+            int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
+            float ms = 0.0f;
+            for (int k = 0; k < 4; ++k) {
+                if (k == 1 && (e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "tune event");
+                if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, 2, h->lossGrid, v, h->queue.p,
+                                        h->stream)) ||
+                    (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream)))
+                    return cuda_fail(e, "tune pass");
+            }
+            if ((e = cudaEventRecord(h->ev1, h->stream)) || (e = cudaEventSynchronize(h->ev1)) ||
+                (e = cudaEventElapsedTime(&ms, h->ev0, h->ev1)))
+                return cuda_fail(e, "tune timing");
+            score[v] = std::min(score[v], ms);
+        }
+    int best = (int)(std::min_element(score.begin(), score.end()) - score.begin());
+    if ((e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * 2 * (size_t)h->numSlots(), h->stream)) ||
+        (e = cudaMemcpyAsync(h->state.p, &saved, sizeof(VmState), cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaStreamSynchronize(h->stream)))
+        return cuda_fail(e, "tune restore");
+    {
+        std::lock_guard<std::mutex> lk(g_tuneMu);
+        g_tuned[bucket] = best;
+    }
+    set_loss_variant(h, best);
+    return upload_tables(h);
 }
 
 int enqueue_build_grid(vm_optimizer *h)
@@ -650,6 +729,10 @@ int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
     if (iterations <= 0 || h->numSlots() == 0 || h->targetCapacity == 0) return VM_OK;
     int rc;
     if ((rc = ensure_grid(h))) return rc;
+    if (h->tunePending) {
+        drop_graph(h);
+        if ((rc = autotune_loss_variant(h))) return rc;
+    }
     if ((rc = ensure_graph(h))) return rc;
     cudaError_t e;
     if ((e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "event");

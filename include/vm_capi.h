@@ -191,8 +191,10 @@ int vmb_memory(vmb_batch *b, size_t *freeBytes, size_t *totalBytes, int *liveFit
  * starts). Arrived requests are admitted in arrival order while the HBM
  * budget and `maxLive` allow; all live fits step together, `stepsPerRound`
  * steps at a time; after each round every live fit's full-target loss is
- * evaluated and the fit retires when it has taken maxSteps steps or its
- * loss changed by less than relTol (relative) since the previous round. A
+ * taken (the loss pass of the round's last step when every live fit uses
+ * sampleFraction 1, else a separate evaluation pass) and the fit retires
+ * when it has taken maxSteps steps or its loss changed by less than relTol
+ * (relative) since the previous round. A
  * retired fit's generators are copied to outGenerators (when non-NULL) and
  * its memory admits the next request. maxLive = 1 is the one-fit-at-a-time
  * loop. Times in vms_result are seconds since the call started. */
