@@ -23,11 +23,9 @@ struct TgtOut {
 
 // Gradient of d^2 for target p, nearest site c0 and bisector neighbour cj,
 // in the reference's operation order (voro_optimizer.cu:245-253).
-__device__ __forceinline__ void grad_terms(float2 p, float2 c0, float2 cj, float bestD, TgtOut &o)
+// u = p - c0, e = cj - c0, l = |e| (sqrtf of ex*ex + ey*ey).
+__device__ __forceinline__ void grad_terms_e(float ux, float uy, float ex, float ey, float l, float bestD, TgtOut &o)
 {
-    float ux = p.x - c0.x, uy = p.y - c0.y;
-    float ex = cj.x - c0.x, ey = cj.y - c0.y;
-    float l = sqrtf(ex * ex + ey * ey);
     float il = 1.0f / l;
     float nx = il * ex, ny = il * ey;
     float un = ux * nx + uy * ny;
@@ -39,6 +37,13 @@ __device__ __forceinline__ void grad_terms(float2 p, float2 c0, float2 cj, float
     o.gjy = s * dcy;
     o.g0x = -s * (nx + dcx);
     o.g0y = -s * (ny + dcy);
+}
+
+__device__ __forceinline__ void grad_terms(float2 p, float2 c0, float2 cj, float bestD, TgtOut &o)
+{
+    float ux = p.x - c0.x, uy = p.y - c0.y;
+    float ex = cj.x - c0.x, ey = cj.y - c0.y;
+    grad_terms_e(ux, uy, ex, ey, sqrtf(ex * ex + ey * ey), bestD, o);
 }
 
 // Fast path: nearest site and bisector argmin from the (2R+1)^2 cell block
@@ -252,8 +257,13 @@ __device__ __forceinline__ int warp_compact(const WarpStage &W, float4 *list, in
 
 // Exact argmin of (d^2, d2, index) over a candidate list, c0 excluded: the
 // rare case where two candidates' error bounds overlap.
-__device__ __noinline__ void list_exact_argmin(const float4 *list, int n, float2 p, int i0, float c0x, float c0y,
-                                               float &bdsq, float &bd, float &bdd, int &bj, int &kb)
+struct ArgMin {
+    float dsq, d, dd; // d^2, d, d2(p, site)
+    int j, k;         // site index (-1: none), staged entry
+};
+
+__device__ __noinline__ ArgMin list_exact_argmin(const float4 *list, int n, float2 p, int i0, float c0x, float c0y,
+                                                 ArgMin b)
 {
     float ux = p.x - c0x, uy = p.y - c0y;
     for (int q = 0; q < n; ++q) {
@@ -267,15 +277,10 @@ __device__ __noinline__ void list_exact_argmin(const float4 *list, int n, float2
         float dsq = d * d;
         float dx = c.x - p.x, dy = c.y - p.y;
         float dd = dx * dx + dy * dy;
-        bool better = bj < 0 ? dsq < FLT_MAX : (dsq < bdsq || (dsq == bdsq && key_less(dd, id, bdd, bj)));
-        if (better) {
-            bdsq = dsq;
-            bd = d;
-            bdd = dd;
-            bj = id;
-            kb = __float_as_int(c.w);
-        }
+        bool better = b.j < 0 ? dsq < FLT_MAX : (dsq < b.dsq || (dsq == b.dsq && key_less(dd, id, b.dd, b.j)));
+        if (better) b = ArgMin{dsq, d, dd, id, __float_as_int(c.w)};
     }
+    return b;
 }
 
 __device__ __noinline__ int staged_rank(const WarpStage &W, int m, float2 p, float bdd, int bj)
@@ -370,7 +375,7 @@ __device__ __forceinline__ void warp_min2(float a, float b, float &m1, float &m2
 // other sites with dmin below the warp's largest such bound.
 __device__ __forceinline__ int loss_staged(const VmFit &F, WarpStage &W, bool take, float2 p, int m2, float bx0,
                                            float bx1, float by0, float by1, int xlo, int xhi, int ylo, int yhi,
-                                           TgtOut &o, float &bddOut)
+                                           TgtOut &o, float &bddOut, bool &rankSure)
 {
     int lane = threadIdx.x & 31;
     float dm[2], dx2[2];
@@ -442,9 +447,11 @@ __device__ __forceinline__ int loss_staged(const VmFit &F, WarpStage &W, bool ta
     T = T < FLT_MAX ? T * T + 1e-30f : FLT_MAX;
     if (!take) T = 0.0f;
     float Tmax = warp_max(T);
+    float listedTo = fmaxf(U2, Tmax); // near and far hold every site with dmin <= listedTo
     int n2 = warp_compact(W, W.far, m2, dm[0] > U2 && dm[0] <= Tmax, dm[1] > U2 && dm[1] <= Tmax);
     __syncwarp();
     for (int q = 0; q < n2; ++q) consider(W.far[q]);
+    bool listedOk = n1 + n2 <= F.K;
     if (!take) return 0;
     if (i0 < 0) return -1;
     // squares of |d| below 1e-18 may round to equal floats: settle exactly
@@ -454,9 +461,14 @@ __device__ __forceinline__ int loss_staged(const VmFit &F, WarpStage &W, bool ta
     float bdsq = FLT_MAX, bd = 0.0f, bdd = 0.0f;
     int bj = -1;
     if (special || lowOther <= best + bestEps) {
-        kb = -1;
-        list_exact_argmin(W.near, n1, p, i0, c0x, c0y, bdsq, bd, bdd, bj, kb);
-        list_exact_argmin(W.far, n2, p, i0, c0x, c0y, bdsq, bd, bdd, bj, kb);
+        ArgMin am{FLT_MAX, 0.0f, 0.0f, -1, -1};
+        am = list_exact_argmin(W.near, n1, p, i0, c0x, c0y, am);
+        am = list_exact_argmin(W.far, n2, p, i0, c0x, c0y, am);
+        bdsq = am.dsq;
+        bd = am.d;
+        bdd = am.dd;
+        bj = am.j;
+        kb = am.k;
     } else if (kb >= 0) {
         float ex = W.x[kb] - c0x, ey = W.y[kb] - c0y;
         float l = sqrtf(ex * ex + ey * ey);
@@ -494,6 +506,9 @@ __device__ __forceinline__ int loss_staged(const VmFit &F, WarpStage &W, bool ta
     o.loss = bdsq;
     grad_terms(p, make_float2(c0x, c0y), make_float2(W.x[kb], W.y[kb]), bd, o);
     bddOut = bdd;
+    // every site nearer p than bj has dmin <= bdd; when bdd is within the
+    // listed range, those sites are all listed, so bj ranks below n1 + n2
+    rankSure = listedOk && bdd <= listedTo;
     return 1;
 }
 
@@ -622,8 +637,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 int ylo = max(lcy - 2, 0), yhi = min(lcy + 2, F.gridH - 1);
                 // writes o only for this group's lanes
                 float bdd = 0.0f;
-                int rg = loss_staged(F, W, mine, p, m2, bx0, bx1, by0, by1, xlo, xhi, ylo, yhi, o, bdd);
-                if (m2 > F.K) {
+                bool rankSure = false;
+                int rg = loss_staged(F, W, mine, p, m2, bx0, bx1, by0, by1, xlo, xhi, ylo, yhi, o, bdd, rankSure);
+                if (m2 > F.K && __any_sync(kFull, mine && rg > 0 && !rankSure)) {
                     // bj must rank below K among all sites; every closer site is staged
                     // (certified), and a site s is closer only if dmin(s) <= d2(p, bj).
                     // One warp vote settles it unless K staged sites are that near.
@@ -641,8 +657,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
             bool deferred = false;
             if (take) {
                 if (pending) {
-                    r = loss_block(F, p, 1, F.K, o);
-                    if (r < 0) r = loss_block(F, p, 2, F.K, o);
+                    TgtOut ob; // its address goes to the out-of-line search; o stays in registers
+                    r = loss_block(F, p, 1, F.K, ob);
+                    if (r < 0) r = loss_block(F, p, 2, F.K, ob);
+                    if (r > 0) o = ob;
                 }
                 if (r < 0) {
                     int q = atomicAdd(&queue->count, 1);
@@ -758,8 +776,8 @@ extern "C++" {
 struct LossVariant {
     int threads, minBlocks;
 };
-static const LossVariant kVariants[] = {{256, 4}, {256, 3}, {256, 2}, {128, 8},
-                                        {128, 6}, {64, 16}, {64, 12}, {512, 2}};
+static const LossVariant kVariants[] = {{256, 4}, {256, 3}, {256, 2}, {128, 5},
+                                        {128, 6}, {64, 16}, {64, 12}, {64, 10}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int vm_loss_variants() { return kNumVariants; }
@@ -773,11 +791,11 @@ static void *variant_fn(int v)
     case 0: return loss_fn<256, 4>();
     case 1: return loss_fn<256, 3>();
     case 2: return loss_fn<256, 2>();
-    case 3: return loss_fn<128, 8>();
+    case 3: return loss_fn<128, 5>();
     case 4: return loss_fn<128, 6>();
     case 5: return loss_fn<64, 16>();
     case 6: return loss_fn<64, 12>();
-    default: return loss_fn<512, 2>();
+    default: return loss_fn<64, 10>();
     }
 }
 
