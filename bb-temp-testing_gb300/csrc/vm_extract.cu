@@ -310,7 +310,30 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
     }
 }
 
+// Cell i's vertices and edge labels from its fixed-size slot to the packed
+// CSR position start[i] (start = exclusive scan of the counts).
+__global__ void __launch_bounds__(256) k_compact_cells(const float2 *__restrict__ verts, const int *__restrict__ labels,
+                                                       const int *__restrict__ start, int n, float2 *__restrict__ outV,
+                                                       int *__restrict__ outL)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int b = start[i], c = start[i + 1] - b;
+    for (int k = 0; k < c; ++k) {
+        outV[b + k] = verts[(size_t)i * kMaxVerts + k];
+        outL[b + k] = labels[(size_t)i * kMaxVerts + k];
+    }
+}
+
 } // namespace vmk
+
+cudaError_t vm_launch_compact_cells(const float2 *verts, const int *labels, const int *start, int n, float2 *outV,
+                                    int *outL, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    vmk::k_compact_cells<<<(n + 255) / 256, 256, 0, s>>>(verts, labels, start, n, outV, outL);
+    return cudaGetLastError();
+}
 
 cudaError_t vm_launch_cells_n(const VmFit *fit, int nSlots, const unsigned long long *masks, int tilesX, int tilesY,
                               float invVoxel, float2 *outVerts, int *outEdges, int *outCount,

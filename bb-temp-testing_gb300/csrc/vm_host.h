@@ -61,7 +61,8 @@ struct MeshHost {
     float gpuMs = 0.0f, hostMs = 0.0f;
 };
 
-void assemble_boundary(const std::vector<float2> &verts, const std::vector<int> &labels,
-                       const std::vector<int> &counts, const std::vector<uint8_t> &inside, int n, MeshHost &mesh);
+// Boundary vertices, edges, watertightness and loops from the packed cells
+// (mesh.cellStart, cellVerts, cellLabels, inside).
+void assemble_boundary(int n, MeshHost &mesh);
 
 } // namespace vmh

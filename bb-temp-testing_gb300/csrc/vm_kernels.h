@@ -33,10 +33,13 @@ cudaError_t vm_launch_knn(const VmFit *fit, const float2 *q, int nq, int K, int 
 int vm_loss_occupancy_blocks(int variant);
 cudaError_t vm_launch_scatter_targets(float2 *targets, const int *slots, const float2 *values, int n, cudaStream_t s);
 
-// Voronoi cells for extraction (vm_extract.cu)
+// Voronoi cells for extraction (vm_extract.cu); vm_launch_compact_cells packs
+// the fixed-size cell slots into CSR order (start: n + 1 offsets).
 cudaError_t vm_launch_cells_n(const VmFit *fit, int nSlots, const unsigned long long *masks, int tilesX, int tilesY,
                               float invVoxel, float2 *outVerts, int *outEdges, int *outCount,
                               unsigned char *outInside, int *flags, cudaStream_t s);
+cudaError_t vm_launch_compact_cells(const float2 *verts, const int *labels, const int *start, int n, float2 *outV,
+                                    int *outL, cudaStream_t s);
 
 // Poisson phase-grid sampler (vm_poisson.cu)
 struct PdParams {

@@ -43,17 +43,10 @@ int floor_log2f(float h)
 }
 
 // Boundary assembly of Extract() (reference voro_optimizer.cu:798-854).
-void assemble_boundary(const std::vector<float2> &verts, const std::vector<int> &labels,
-                       const std::vector<int> &counts, const std::vector<uint8_t> &inside, int n, MeshHost &mesh)
+void assemble_boundary(int n, MeshHost &mesh)
 {
-    mesh.cellStart.assign((size_t)n + 1, 0);
-    for (int i = 0; i < n; ++i) mesh.cellStart[i + 1] = mesh.cellStart[i] + counts[i];
-    mesh.cellVerts.resize((size_t)mesh.cellStart[n]);
-    mesh.cellLabels.resize((size_t)mesh.cellStart[n]);
-    for (int i = 0; i < n; ++i) {
-        std::copy_n(verts.begin() + (size_t)i * kMaxCellVerts, counts[i], mesh.cellVerts.begin() + mesh.cellStart[i]);
-        std::copy_n(labels.begin() + (size_t)i * kMaxCellVerts, counts[i], mesh.cellLabels.begin() + mesh.cellStart[i]);
-    }
+    const std::vector<uint8_t> &inside = mesh.inside;
+    auto count = [&](int i) { return mesh.cellStart[i + 1] - mesh.cellStart[i]; };
     // vertex key: the sorted generator triple (labels offset by the 4 box sides, 21 bits each)
     auto key = [](int a, int b, int c) {
         uint64_t v0 = uint64_t(a + 4), v1 = uint64_t(b + 4), v2 = uint64_t(c + 4);
@@ -64,7 +57,7 @@ void assemble_boundary(const std::vector<float2> &verts, const std::vector<int> 
     };
     size_t maxEdges = 0;
     for (int i = 0; i < n; ++i)
-        if (inside[i]) maxEdges += (size_t)counts[i];
+        if (inside[i]) maxEdges += (size_t)count(i);
     size_t cap = 64;
     while (cap < 4 * (maxEdges + 16)) cap <<= 1;
     std::vector<uint64_t> keys(cap);
@@ -86,9 +79,9 @@ void assemble_boundary(const std::vector<float2> &verts, const std::vector<int> 
     mesh.edges.clear();
     for (int i = 0; i < n; ++i) {
         if (!inside[i]) continue;
-        int c = counts[i];
-        const int *lab = labels.data() + (size_t)i * kMaxCellVerts;
-        const float2 *pos = verts.data() + (size_t)i * kMaxCellVerts;
+        int c = count(i);
+        const int *lab = mesh.cellLabels.data() + mesh.cellStart[i];
+        const float2 *pos = mesh.cellVerts.data() + mesh.cellStart[i];
         for (int k = 0; k < c; ++k) {
             int l = lab[k];
             if (l >= 0 && inside[l]) continue;
@@ -157,7 +150,9 @@ struct vm_optimizer {
     DevBuf<unsigned long long> occ;
     DevBuf<VmState> state;
     DevBuf<VmFit> dFit;
-    DevBuf<VmPointSet> dSites, dTargets;
+    DevBuf<VmPointSet> dSites, dTargets, dCsrSet;
+    DevBuf<int> cellStartD, csrTiles, csrLabels, dCsrPre; // extraction: cells packed in CSR order
+    DevBuf<float2> csrVerts;
     DevBuf<int> dPre; // [0, siteBlocks, 0, tiles, 0, lossTiles, 0, targetBlocks]
     DevBuf<int> dTPre; // [0, targetBlocks, 0, targetKeyTiles]
     DevBuf<int> tcounts, tstart, ttileSums; // target sort by sub-cell (only while sorting)
@@ -992,15 +987,39 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
         return cuda_fail(e, "extract");
     cudaEventElapsedTime(&h->mesh.gpuMs, h->ev0, h->ev1);
     auto t0 = std::chrono::steady_clock::now();
-    std::vector<float2> verts((size_t)n * kMaxCellVerts);
-    std::vector<int> labels((size_t)n * kMaxCellVerts), counts(n);
-    int flags[2];
+    // pack the cells in CSR order on the device (scan of the counts, then a
+    // gather), so only the used vertex slots cross to the host
+    int tiles = (n + kScanTile - 1) / kScanTile;
+    VmPointSet C{};
+    C.gridW = n;
+    C.gridH = 1;
+    C.counts = h->cellCount.p;
+    int pre[2] = {0, tiles};
+    if ((rc = h->cellStartD.reserve((size_t)n + 1)) || (rc = h->csrTiles.reserve((size_t)tiles + 1)) ||
+        (rc = h->dCsrSet.reserve(1)) || (rc = h->dCsrPre.reserve(2)))
+        return rc;
+    C.start = h->cellStartD.p;
+    C.tileSums = h->csrTiles.p;
+    int total = 0, flags[2];
+    if ((e = cudaMemcpyAsync(h->dCsrSet.p, &C, sizeof(C), cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->dCsrPre.p, pre, sizeof(pre), cudaMemcpyHostToDevice, h->stream)) ||
+        (e = vm_launch_scan(h->dCsrSet.p, h->dCsrPre.p, 1, tiles, h->stream)) ||
+        (e = cudaMemcpyAsync(&total, h->cellStartD.p + n, sizeof(int), cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaStreamSynchronize(h->stream)))
+        return cuda_fail(e, "extract pack");
+    if ((rc = h->csrVerts.reserve(std::max(total, 1))) || (rc = h->csrLabels.reserve(std::max(total, 1)))) return rc;
+    if ((e = vm_launch_compact_cells(h->cellVerts.p, h->cellEdges.p, h->cellStartD.p, n, h->csrVerts.p,
+                                     h->csrLabels.p, h->stream)))
+        return cuda_fail(e, "extract pack");
     MeshHost &M = h->mesh;
     M.generators.resize(n);
     M.inside.resize(n);
-    if ((e = cudaMemcpyAsync(verts.data(), h->cellVerts.p, sizeof(float2) * verts.size(), cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(labels.data(), h->cellEdges.p, sizeof(int) * labels.size(), cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(counts.data(), h->cellCount.p, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream)) ||
+    M.cellStart.resize((size_t)n + 1);
+    M.cellVerts.resize((size_t)total);
+    M.cellLabels.resize((size_t)total);
+    if ((e = cudaMemcpyAsync(M.cellStart.data(), h->cellStartD.p, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, h->stream)) ||
+        (total && (e = cudaMemcpyAsync(M.cellVerts.data(), h->csrVerts.p, sizeof(float2) * (size_t)total, cudaMemcpyDeviceToHost, h->stream))) ||
+        (total && (e = cudaMemcpyAsync(M.cellLabels.data(), h->csrLabels.p, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, h->stream))) ||
         (e = cudaMemcpyAsync(M.inside.data(), h->inside.p, n, cudaMemcpyDeviceToHost, h->stream)) ||
         (e = cudaMemcpyAsync(M.generators.data(), h->gen.p, sizeof(float2) * n, cudaMemcpyDeviceToHost, h->stream)) ||
         (e = cudaMemcpyAsync(flags, h->flags.p, sizeof(flags), cudaMemcpyDeviceToHost, h->stream)) ||
@@ -1008,7 +1027,7 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
         return cuda_fail(e, "extract read");
     M.unsafeCells = flags[0];
     M.overflowCells = flags[1];
-    assemble_boundary(verts, labels, counts, M.inside, n, M);
+    assemble_boundary(n, M);
     M.hostMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     info->numGenerators = n;
     info->numCellVerts = (int)M.cellVerts.size();

@@ -54,8 +54,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
-    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve"],
-                    help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads")
+    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract"],
+                    help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads; "
+                         "extract: the cell clipper")
     ap.add_argument("--fits", type=int, default=512)
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--requests", type=int, default=200)
@@ -242,6 +243,39 @@ def run_batch(args):
                       "unit": "fits/s", "data": "synthetic"}), flush=True)
 
 
+def run_extract(args):
+    """Mesh extraction: the Voronoi-cell clipper (GPU) and the boundary
+    assembly (host) on the 1M-site fit after 50 steps, and on the 512x512
+    lattice with 1e-6 jitter (near-cocircular bisectors). cells/s = sites / clipper GPU time."""
+    import voromesh_gb300 as vm
+    from voromesh_gb300 import synth
+
+    def measure(spec, steps):
+        p = vm.OptimizerParams(iterations=spec.steps, sampleFraction=1.0, lrPerSpacing=spec.lrPerSpacing,
+                               lossK=spec.lossK)
+        o = vm.VoroOptimizer(spec.width, spec.height, spec.spacing, p)
+        o.SetTargets(spec.targets)
+        o.SetGenerators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
+        if steps:
+            o.Step(steps)
+        o.Extract()  # warm-up
+        runs = [o.Extract() for _ in range(3)]
+        o.close()
+        m = min(runs, key=lambda r: r.gpuMs)
+        n = int((m.generators[:, 0] >= 0).sum())
+        return {"sites": n, "steps_before": steps, "clipper_gpu_ms": m.gpuMs, "cells_per_s": n / (m.gpuMs / 1e3),
+                "host_assembly_ms": min(r.hostMs for r in runs), "watertight": bool(m.watertight), "loops": m.loops,
+                "unsafe_cells": m.unsafeCells, "overflow_cells": m.overflowCells,
+                "cell_verts": int(len(m.cellVerts)), "edges": int(len(m.edges))}
+
+    s = vm.Sampler(2.0, 2.0, RADIUS, 30, 1)
+    cells = s.Cells()
+    s.close()
+    out = {"scale_1m": measure(make_inputs(cells), 50), "precision_262k": measure(synth.precision_fit(), 0)}
+    print(json.dumps({"metric": "cells/s, Voronoi-cell clipper (Extract)", "unit": "cells/s",
+                      "value": out["scale_1m"]["cells_per_s"], "workloads": out, "data": "synthetic"}), flush=True)
+
+
 def run_serve(args):
     """Served stream: Poisson arrivals, generators log-uniform in [1k, 1M],
     8x targets from the ellipse-union or star shapes (coin flip), retire at
@@ -299,6 +333,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "extract":
+        run_extract(args)
         return
     import torch
 
