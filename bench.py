@@ -443,7 +443,7 @@ def main():
                        "poisson_fill": {"samples": n_samples, "ms": fill_ms, "samples_per_s": n_samples / (fill_ms / 1e3)},
                        "stage_ms": {"loss": float(stages[0]), "adam_bin": float(stages[1]),
                                     "scan": float(stages[2]), "scatter": float(stages[3])},
-                       "exact_path_targets": int(info.exactTargets)},
+                       "exact_path_targets": int(info.exactTargets), "loss_variant": opt.LossVariant()[0]},
             "e2e": {"value": e2e, "unit": "site-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": "k_loss", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
