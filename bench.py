@@ -54,9 +54,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
-    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract"],
+    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit"],
                     help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads; "
-                         "extract: the cell clipper")
+                         "extract: the cell clipper; edit: the local-edit pipeline")
     ap.add_argument("--fits", type=int, default=512)
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--requests", type=int, default=200)
@@ -293,6 +293,107 @@ def run_extract(args):
                       "value": out["scale_1m"]["cells_per_s"], "workloads": out, "data": "synthetic"}), flush=True)
 
 
+def run_edit(args):
+    """The local-edit pipeline of the reference's editor (Editor::Stamp,
+    apps/voromesh_demo.cpp:117-156) with its defaults: a 1024 x 1024 domain,
+    1-unit voxels, Poisson radius 24 (61 x 61 generator slots), 100 local
+    steps, sample fraction 0.2. The canvas is a stand-in: the object is a
+    union of discs, its surface targets lie on the outline at unit spacing,
+    and each edit adds a disc of radius 40 on the outline. Each stamp runs
+    UpdateTargets + UpdateOccupancy, a region Resample + UpdateGenerators,
+    BeginSchedule on the region + Optimize, and Extract; wall ms per phase."""
+    import voromesh_gb300 as vm
+
+    domain, voxel, radius, brush = 1024.0, 1.0, 24.0, 40.0
+    discs = [(512.0, 512.0, 300.0)]
+
+    def inside(x, y):
+        r = np.zeros(np.broadcast(x, y).shape, bool)
+        for cx, cy, rr in discs:
+            r |= (x - cx) ** 2 + (y - cy) ** 2 < rr * rr
+        return r
+
+    def rim(cx, cy, rr):
+        n = int(np.ceil(2 * np.pi * rr))
+        t = np.arange(n) * (2 * np.pi / n)
+        return np.stack([cx + rr * np.cos(t), cy + rr * np.sin(t)], 1).astype(np.float32)
+
+    nv = int(domain / voxel)
+    tiles = nv // 8
+    vc = (np.arange(nv) + 0.5) * voxel
+
+    def masks_of():
+        ins = inside(vc[None, :], vc[:, None])  # [y, x]
+        bits = ins.reshape(tiles, 8, tiles, 8).transpose(0, 2, 1, 3).reshape(tiles, tiles, 64).astype(np.uint64)
+        return (bits << np.arange(64, dtype=np.uint64)).sum(axis=2, dtype=np.uint64).reshape(-1)
+
+    slots = rim(*discs[0])
+    params = vm.OptimizerParams()  # iterations 400, localIterations 100, sampleFraction 0.2
+    opt = vm.VoroOptimizer(domain, domain, radius, params)
+    t0 = time.perf_counter()
+    opt.SetTargets(slots)
+    masks = masks_of()
+    opt.SetOccupancy(masks, tiles, tiles, voxel)
+    sampler = vm.Sampler(domain, domain, radius, 30, 1)
+    opt.SetGenerators(sampler.Cells(), sampler.GridW(), sampler.GridH(), sampler.CellSize())
+    global_gpu = opt.Optimize()
+    opt.Extract()
+    reset_ms = (time.perf_counter() - t0) * 1e3
+    rows = []
+    n_stamps = 21
+    for k in range(n_stamps):
+        th = 2 * np.pi * k / n_stamps
+        cx, cy = 512.0 + 300.0 * np.cos(th), 512.0 + 300.0 * np.sin(th)
+        ta = time.perf_counter()
+        # canvas stand-in: drop targets inside the new disc, add its rim outside the object
+        live = slots[:, 0] >= 0
+        gone = live & ((slots[:, 0] - cx) ** 2 + (slots[:, 1] - cy) ** 2 < brush * brush)
+        new = rim(cx, cy, brush)
+        new = new[~inside(new[:, 0], new[:, 1])]
+        discs.append((cx, cy, brush))
+        slots[gone] = -1.0
+        free = np.flatnonzero(slots[:, 0] < 0)
+        if len(free) < len(new):
+            slots = np.concatenate([slots, np.full((len(new) - len(free), 2), -1.0, np.float32)])
+            free = np.flatnonzero(slots[:, 0] < 0)
+        slots[free[:len(new)]] = new
+        dirty = np.concatenate([np.flatnonzero(gone), free[:len(new)]]).astype(np.int32)
+        masks = masks_of()
+        tx0, ty0 = int((cx - brush) // (8 * voxel)), int((cy - brush) // (8 * voxel))
+        tx1, ty1 = int(np.ceil((cx + brush) / (8 * voxel))), int(np.ceil((cy + brush) / (8 * voxel)))
+        tb = time.perf_counter()
+        opt.UpdateTargets(dirty, slots)
+        opt.UpdateOccupancy(masks, max(tx0, 0), max(ty0, 0), min(tx1, tiles), min(ty1, tiles))
+        tc = time.perf_counter()
+        margin, cs = brush + 2 * radius, sampler.CellSize()
+        rx0, ry0 = max(int(np.floor((cx - margin) / cs)), 0), max(int(np.floor((cy - margin) / cs)), 0)
+        rx1 = min(int(np.ceil((cx + margin) / cs)), sampler.GridW())
+        ry1 = min(int(np.ceil((cy + margin) / cs)), sampler.GridH())
+        pgpu = sampler.Resample(rx0, ry0, rx1, ry1)
+        opt.UpdateGenerators(sampler.Cells(), rx0, ry0, rx1, ry1)
+        td = time.perf_counter()
+        opt.BeginSchedule(params.localIterations, rx0, ry0, rx1, ry1)
+        ogpu = opt.Optimize()
+        te = time.perf_counter()
+        mesh = opt.Extract()
+        tf = time.perf_counter()
+        if k:  # the first stamp warms up
+            rows.append({"canvas": (tb - ta) * 1e3, "upload": (tc - tb) * 1e3, "poisson": (td - tc) * 1e3,
+                         "optimize": (te - td) * 1e3, "extract": (tf - te) * 1e3, "total_pipeline": (tf - tb) * 1e3,
+                         "poisson_gpu": pgpu, "optimize_gpu": ogpu, "extract_gpu": mesh.gpuMs,
+                         "slots": (rx1 - rx0) * (ry1 - ry0)})
+    sampler.close()
+    opt.close()
+    med = {key: float(np.median([r[key] for r in rows])) for key in rows[0]}
+    print(json.dumps({"metric": "ms per local edit (p50), Editor::Stamp pipeline", "unit": "ms",
+                      "value": med["total_pipeline"], "higher_is_better": False,
+                      "workload": "1024^2 domain, 1-unit voxels, Poisson r=24 (61x61 slots), 100 local steps, "
+                                  "sampleFraction 0.2, disc-union canvas stand-in, brush radius 40",
+                      "p50_ms": med, "p99_total_ms": float(np.percentile([r["total_pipeline"] for r in rows], 99)),
+                      "stamps": len(rows), "reset_and_global_fit_ms": reset_ms, "global_fit_gpu_ms": global_gpu,
+                      "data": "synthetic"}), flush=True)
+
+
 def run_serve(args):
     """Served stream: Poisson arrivals, generators log-uniform in [1k, 1M],
     8x targets from the ellipse-union or star shapes (coin flip), retire at
@@ -353,6 +454,9 @@ def main():
         return
     if args.workload == "extract":
         run_extract(args)
+        return
+    if args.workload == "edit":
+        run_edit(args)
         return
     import torch
 
