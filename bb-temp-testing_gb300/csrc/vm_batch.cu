@@ -141,7 +141,6 @@ int single_set_build(vmb_batch *b, const VmPointSet &S, int emptyIsNegative, int
         (e = vm_launch_bin(b->dOneSet.p, b->dOnePre.p, 1, blocks, emptyIsNegative, b->stream)) ||
         (e = vm_launch_scan(b->dOneSet.p, b->dOnePre.p + 2, 1, tiles, b->stream)) ||
         (e = vm_launch_scatter(b->dOneSet.p, b->dOnePre.p, 1, blocks, nullptr, b->stream)) ||
-        (e = vm_launch_canonical(b->dOneSet.p, b->dOnePre.p + 2, 1, tiles, b->stream)) ||
         (e = cudaStreamSynchronize(b->stream))) // the tables above live on the host stack
         return cuda_fail(e, "batch grid build");
     return VM_OK;
@@ -199,8 +198,7 @@ int enqueue_batch_step(vmb_batch *b)
                             b->stream)) ||
         (e = vm_launch_adam_bin(b->dFits.p, sitePre, nf, b->siteBlocks, b->queue.p, b->stream)) ||
         (e = vm_launch_scan(b->dSites.p, scanPre, nf, b->scanTiles, b->stream)) ||
-        (e = vm_launch_scatter(b->dSites.p, sitePre, nf, b->siteBlocks, b->dFits.p, b->stream)) ||
-        (e = vm_launch_canonical(b->dSites.p, scanPre, nf, b->scanTiles, b->stream)))
+        (e = vm_launch_scatter(b->dSites.p, sitePre, nf, b->siteBlocks, b->dFits.p, b->stream)))
         return cuda_fail(e, "batch step");
     return VM_OK;
 }

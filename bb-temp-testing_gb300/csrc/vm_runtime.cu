@@ -131,6 +131,7 @@ struct vm_optimizer {
     int iteration = 0, scheduleLength = 0;
     float lastBatchLoss = 0;
     bool gridValid = false;
+    bool gridCanonical = false; // each cell's run sorted by slot (needed only when exported)
     int lossGrid = 0;
     int lossTile = 256;    // targets per loss tile (= its block size)
     int lossVariant = 3;   // loss kernel variant in use
@@ -316,7 +317,7 @@ int enqueue_build_grid(vm_optimizer *h)
     if ((e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "scan");
     if ((e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, nullptr, h->stream)))
         return cuda_fail(e, "scatter");
-    if ((e = vm_launch_canonical(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "canonical");
+    h->gridCanonical = false;
     return VM_OK;
 }
 
@@ -341,7 +342,6 @@ int enqueue_step(vm_optimizer *h)
     if ((e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "scan");
     if ((e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, h->dFit.p, h->stream)))
         return cuda_fail(e, "scatter");
-    if ((e = vm_launch_canonical(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "canonical");
     return VM_OK;
 }
 
@@ -731,6 +731,7 @@ int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
     if ((rc = ensure_graph(h))) return rc;
     cudaError_t e;
     if ((e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "event");
+    h->gridCanonical = false; // the steps rebuild the grid
     for (int k = 0; k < iterations; ++k)
         if ((e = cudaGraphLaunch(h->graph, h->stream))) return cuda_fail(e, "graph launch");
     if ((e = cudaEventRecord(h->ev1, h->stream))) return cuda_fail(e, "event");
@@ -761,6 +762,7 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
     }
     int n = h->numSlots();
     int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
+    h->gridCanonical = false; // the steps rebuild the grid
     for (int k = 0; k < iterations; ++k) {
         cudaEvent_t *ev = &h->timing[(size_t)k * 5];
         if ((e = cudaEventRecord(ev[0], h->stream)) ||
@@ -771,7 +773,6 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
             (e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream)) ||
             (e = cudaEventRecord(ev[3], h->stream)) ||
             (e = vm_launch_scatter(h->dSites.p, h->dPre.p + 0, 1, (n + 255) / 256, h->dFit.p, h->stream)) ||
-            (e = vm_launch_canonical(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream)) ||
             (e = cudaEventRecord(ev[4], h->stream)))
             return cuda_fail(e, "timed step");
     }
@@ -873,8 +874,16 @@ int vm_get_grid(vm_optimizer *h, int *start, int *sortedIdx, float *sortedPos, i
     int rc;
     if (h->numSlots() == 0) return VM_OK;
     if ((rc = ensure_grid(h))) return rc;
+    cudaError_t e;
+    if (!h->gridCanonical) {
+        // the step leaves each cell's run in arrival order (nothing in the step
+        // depends on it); the exported grid is in ascending slot order
+        if ((e = vm_launch_canonical(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream)))
+            return cuda_fail(e, "canonical");
+        h->gridCanonical = true;
+    }
     int live = 0;
-    cudaError_t e = cudaMemcpyAsync(&live, h->start.p + h->cells, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    e = cudaMemcpyAsync(&live, h->start.p + h->cells, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
     if (!e) e = cudaStreamSynchronize(h->stream);
     if (!e && start) e = cudaMemcpyAsync(start, h->start.p, sizeof(int) * (size_t)(h->cells + 1), cudaMemcpyDeviceToHost, h->stream);
     if (!e && sortedIdx) e = cudaMemcpyAsync(sortedIdx, h->sortedIdx.p, sizeof(int) * (size_t)live, cudaMemcpyDeviceToHost, h->stream);

@@ -4,7 +4,7 @@
 //   k_scan_tiles   per-tile sums of the cell counts          (reference cub ExclusiveSum, :697)
 //   k_scan_apply   exclusive scan -> cell start
 //   k_scatter      cell-sorted copy (reference scatterKernel :179-187)
-//   k_canonical    each cell's run sorted by slot index, so the order is canonical
+//   k_canonical    each cell's run sorted by slot index (before the grid is exported)
 //   (k_loss        VoroLoss + analytic gradient per target, vm_loss.cu)
 //   k_adam_bin     Adam + clamp, fused with the next step's binning (reference
 //                  adamKernel :271-301 + binKernel); its lr and bias corrections
@@ -13,9 +13,11 @@
 //   k_knn          exact kNN query operator (reference knn<K>, :130-163)
 //
 // One step of a set of fits is: k_loss -> k_adam_bin -> k_scan_tiles ->
-// k_scan_apply -> k_scatter(publish) -> k_canonical. The grid is therefore always built for
+// k_scan_apply -> k_scatter(publish). The grid is therefore always built for
 // the current generators between steps, as the reference rebuilds it at the
-// start of each step.
+// start of each step. Nothing in the step depends on the order within a
+// cell's run (every argmin breaks ties by index, every sum is exact), so
+// k_canonical runs only before the grid is exported.
 #include "vm_device.cuh"
 #include "vm_grid.cuh"
 #include "vm_knn.cuh"

@@ -44,7 +44,7 @@ N_TARGETS = 8388608
 K = 16
 RADIUS = 1e-3
 LR_PER_SPACING = 0.09
-KERNELS_PER_STEP = 7  # k_loss, k_loss_exact, k_adam_bin, k_scan_tiles, k_scan_apply, k_scatter, k_canonical
+KERNELS_PER_STEP = 6  # k_loss, k_loss_exact, k_adam_bin, k_scan_tiles, k_scan_apply, k_scatter
 
 
 def parse():
