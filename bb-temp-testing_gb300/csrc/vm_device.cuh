@@ -154,40 +154,6 @@ __device__ __forceinline__ void atomic_add128(unsigned long long *lo, unsigned l
     if (vhi) atomicAdd(hi, vhi);
 }
 
-// Sum of x over the lanes of `peers` (lanes sharing one key), delivered to
-// the lowest lane of the group. Tree over relative positions within the
-// group; integer addition makes it exact. All 32 lanes must call it.
-__device__ __forceinline__ long long reduce_peers(unsigned peers, long long x)
-{
-    int lane = threadIdx.x & 31;
-    int rel = __popc(peers & ((1u << lane) - 1u));
-    unsigned rest = peers & (0xFFFFFFFEu << lane);
-    for (;;) {
-        if (!__any_sync(kFull, rest != 0)) break;
-        int next = __ffs(rest);
-        long long t = __shfl_sync(kFull, x, next > 0 ? next - 1 : lane);
-        if (next) x += t;
-        unsigned done = __ballot_sync(kFull, (rel & 1) != 0);
-        rest &= ~done;
-        rel >>= 1;
-    }
-    return x;
-}
-
-// Warp-aggregated int64 add of (vx, vy) into acc[2*key], acc[2*key+1] for
-// every lane with key >= 0. All 32 lanes must call it.
-__device__ __forceinline__ void warp_add_pair(long long *acc, int key, long long vx, long long vy)
-{
-    unsigned peers = __match_any_sync(kFull, key);
-    long long sx = reduce_peers(peers, vx);
-    long long sy = reduce_peers(peers, vy);
-    int lane = threadIdx.x & 31;
-    if (key >= 0 && lane == __ffs(peers) - 1) {
-        if (sx) atomicAdd(reinterpret_cast<unsigned long long *>(&acc[2 * (size_t)key]), (unsigned long long)sx);
-        if (sy) atomicAdd(reinterpret_cast<unsigned long long *>(&acc[2 * (size_t)key + 1]), (unsigned long long)sy);
-    }
-}
-
 // Block index -> fit index by binary search in prefix[0..nFits] (prefix[0]=0).
 __device__ __forceinline__ int find_fit(const int *prefix, int nFits, int b)
 {

@@ -19,7 +19,7 @@ cudaError_t vm_launch_canonical(const VmPointSet *sets, const int *tilePrefix, i
 // queue (created by vm_queue_init; items hold (fit, target) int2 pairs).
 // `variant` picks block size and occupancy target; its block size is also the
 // number of targets per tile the prefix table counts.
-cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode, int maxR,
+cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode,
                            int gridBlocks, int variant, void *queue, cudaStream_t s);
 int vm_loss_variants();
 int vm_loss_variant_threads(int variant);

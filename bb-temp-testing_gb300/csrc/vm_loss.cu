@@ -562,8 +562,7 @@ __device__ __forceinline__ void run_add(RunSum &r, int site, long long x, long l
 // the few sites some lane can need.
 template <int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB)
-    k_loss(const VmFit *__restrict__ fits, const int *__restrict__ prefix, int nFits, int mode, int maxR,
-           SlowQueue *queue)
+    k_loss(const VmFit *__restrict__ fits, const int *__restrict__ prefix, int nFits, int mode, SlowQueue *queue)
 {
     constexpr int NW = THREADS / 32;
     constexpr int kGroups = 3; // cell groups per warp and iteration on the staged path
@@ -799,14 +798,14 @@ static void *variant_fn(int v)
     }
 }
 
-cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode, int maxR,
+cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode,
                            int gridBlocks, int variant, void *queue, cudaStream_t s)
 {
     if (totalTiles <= 0) return cudaSuccess;
     int g = gridBlocks < totalTiles ? gridBlocks : totalTiles;
     if (g < 1) g = 1;
     SlowQueue *q = static_cast<SlowQueue *>(queue);
-    void *args[] = {(void *)&fits, (void *)&tilePrefix, (void *)&nFits, (void *)&mode, (void *)&maxR, (void *)&q};
+    void *args[] = {(void *)&fits, (void *)&tilePrefix, (void *)&nFits, (void *)&mode, (void *)&q};
     cudaError_t e = cudaLaunchKernel(variant_fn(variant), dim3(g), dim3(vm_loss_variant_threads(variant)), args, 0, s);
     if (e) return e;
     int sms = 0, dev = 0;

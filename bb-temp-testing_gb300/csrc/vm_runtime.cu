@@ -286,7 +286,7 @@ int autotune_loss_variant(vm_optimizer *h)
             float ms = 0.0f;
             for (int k = 0; k < 4; ++k) {
                 if (k == 1 && (e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "tune event");
-                if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, 2, h->lossGrid, v, h->queue.p,
+                if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, v, h->queue.p,
                                         h->stream)) ||
                     (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream)))
                     return cuda_fail(e, "tune pass");
@@ -335,7 +335,7 @@ int enqueue_step(vm_optimizer *h)
     int n = h->numSlots();
     cudaError_t e;
     int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
-    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)))
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, h->lossVariant, h->queue.p, h->stream)))
         return cuda_fail(e, "loss");
     if ((e = vm_launch_adam_bin(h->dFit.p, h->dPre.p + 0, 1, (n + 255) / 256, h->queue.p, h->stream)))
         return cuda_fail(e, "adam");
@@ -766,7 +766,7 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
     for (int k = 0; k < iterations; ++k) {
         cudaEvent_t *ev = &h->timing[(size_t)k * 5];
         if ((e = cudaEventRecord(ev[0], h->stream)) ||
-            (e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+            (e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
             (e = cudaEventRecord(ev[1], h->stream)) ||
             (e = vm_launch_adam_bin(h->dFit.p, h->dPre.p + 0, 1, (n + 255) / 256, h->queue.p, h->stream)) ||
             (e = cudaEventRecord(ev[2], h->stream)) ||
@@ -821,7 +821,7 @@ int vm_evaluate_loss(vm_optimizer *h, float *loss)
     if ((rc = ensure_grid(h))) return rc;
     cudaError_t e;
     int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
-    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 1, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 1, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
         (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream)))
         return cuda_fail(e, "evaluate loss");
     VmState st;
@@ -932,7 +932,7 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
     if ((rc = upload_tables(h))) return rc;
     cudaError_t e;
     int lossTiles = (live + h->lossTile - 1) / h->lossTile;
-    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, mode, 2, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, mode, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
         (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream))) {
         h->fit = saved;
         upload_tables(h);
