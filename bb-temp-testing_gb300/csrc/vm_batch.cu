@@ -596,11 +596,15 @@ int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result 
     std::vector<int> liveReq(b->maxFits, -1); // fit id -> request
     std::vector<float> prevLoss(b->maxFits, -1.0f), losses(b->maxFits, 0.0f);
     std::vector<int> steps(b->maxFits, 0);
-    size_t head = 0;
+    size_t head = 0, liveTargets = 0;
     int done = 0, live = 0;
+    auto targetsOf = [&](int r) { return (size_t)std::max(reqs[r].fit.nTargets, 0); };
     while (done < n) {
-        // admit every arrived request that fits (FIFO; the head waits for memory)
-        while (head < pending.size() && reqs[pending[head]].arrival <= now() && live < cfg->maxLive) {
+        // admit every arrived request that fits (FIFO; the head waits for memory
+        // and, under a target cap, for live work to retire)
+        while (head < pending.size() && reqs[pending[head]].arrival <= now() && live < cfg->maxLive &&
+               (live == 0 || cfg->maxLiveTargets == 0 ||
+                liveTargets + targetsOf(pending[head]) <= cfg->maxLiveTargets)) {
             int r = pending[head], id = -1;
             rc = vmb_add_fit(b, &reqs[r].fit, &id);
             if (rc == VM_ERR_BUDGET) {
@@ -618,6 +622,7 @@ int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result 
                 return rc;
             }
             res[r].admitted = now();
+            liveTargets += targetsOf(r);
             liveReq[id] = r;
             prevLoss[id] = -1.0f;
             steps[id] = 0;
@@ -655,6 +660,7 @@ int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result 
                 res[r].finalLoss = L;
                 res[r].status = VM_OK;
                 vmb_remove_fit(b, id);
+                liveTargets -= targetsOf(r);
                 liveReq[id] = -1;
                 --live;
                 ++done;

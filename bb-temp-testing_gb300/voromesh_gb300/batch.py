@@ -33,7 +33,7 @@ class vms_request(C.Structure):
 
 class vms_config(C.Structure):
     _fields_ = [("hbmBudgetBytes", C.c_size_t), ("maxLive", C.c_int), ("stepsPerRound", C.c_int),
-                ("lossVariant", C.c_int)]
+                ("lossVariant", C.c_int), ("maxLiveTargets", C.c_size_t)]
 
 
 class vms_result(C.Structure):
@@ -156,9 +156,11 @@ class ServeResult:
 
 
 def serve(specs, arrivals, hbm_budget: int, max_live: int = 1024, steps_per_round: int = 10, max_steps: int = 500,
-          rel_tol: float = 1e-6, loss_variant: int = -1, keep_generators: bool = True) -> ServeResult:
+          rel_tol: float = 1e-6, loss_variant: int = -1, keep_generators: bool = True,
+          max_live_targets: int = 0) -> ServeResult:
     """Serves fit requests arriving at `arrivals` (seconds); maxLive=1 is the
-    one-fit-at-a-time loop."""
+    one-fit-at-a-time loop; max_live_targets caps the live fits' targets (0 =
+    no cap)."""
     lib = _declare(load())
     n = len(specs)
     reqs = (vms_request * max(n, 1))()
@@ -174,7 +176,7 @@ def serve(specs, arrivals, hbm_budget: int, max_live: int = 1024, steps_per_roun
             reqs[i].outGenerators = out.ctypes.data
         else:
             outs.append(None)
-    cfg = vms_config(hbm_budget, max_live, steps_per_round, loss_variant)
+    cfg = vms_config(hbm_budget, max_live, steps_per_round, loss_variant, max_live_targets)
     res = (vms_result * max(n, 1))()
     check(lib.vms_serve(reqs, n, C.byref(cfg), res), "vms_serve")
     arr = lambda f, dt: np.array([getattr(res[i], f) for i in range(n)], dt)

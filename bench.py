@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--serve-budget-gb", type=int, default=64)
+    ap.add_argument("--serve-max-targets", type=int, default=1 << 24,
+                    help="live-target cap of the served stream's admission (0 = none)")
     return ap.parse_args()
 
 
@@ -426,16 +428,20 @@ def run_serve(args):
     budget = args.serve_budget_gb << 30
     need = max(fit_bytes(s) for s in specs)
     out = {}
-    for name, live in (("batched", 4096), ("plain_loop", 1)):
+    # batched: admission by memory alone (throughput); batched_capped: a live-target
+    # cap as well, so early requests finish sooner (latency)
+    runs = (("batched", 4096, 0), ("batched_capped", 4096, args.serve_max_targets), ("plain_loop", 1, 0))
+    for name, live, cap in runs:
         r = serve(specs, arrivals, budget, max_live=live, steps_per_round=10, max_steps=500, rel_tol=1e-6,
-                  keep_generators=False)
+                  keep_generators=False, max_live_targets=cap)
         lat = r.latency
         span = float(r.finished.max() - r.arrival.min())
         out[name] = {"fits_per_s": n / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99), "span_s": span,
                      "mean_steps": float(r.steps.mean()), "rejected": int((r.status != 0).sum())}
     print(json.dumps({"metric": "fits/s + p50/p99, served stream", "workload": f"{n} requests, Poisson arrivals "
                       f"{args.rate}/s, generators log-uniform [1k, 1M], 8x targets (ellipse union or star), retire at "
-                      f"500 steps or rel loss change < 1e-6, HBM budget {args.serve_budget_gb} GiB", **out,
+                      f"500 steps or rel loss change < 1e-6, HBM budget {args.serve_budget_gb} GiB "
+                      f"(batched_capped: live targets capped at {args.serve_max_targets})", **out,
                       "speedup": out["batched"]["fits_per_s"] / out["plain_loop"]["fits_per_s"],
                       "largest_fit_bytes": need, "unit": "fits/s", "data": "synthetic"}), flush=True)
 

@@ -111,9 +111,10 @@ int vm_step(vm_optimizer *h, int iterations, float *gpuMs);
  * queue), Adam + binning, cell-count scan, cell-sorted scatter. An addition
  * (no counterpart in the reference) used to attribute step time. */
 int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs);
-/* Loss-kernel variant (block size, occupancy target, gradient aggregation):
- * -1 = automatic. All variants produce identical results; the autotuner
- * picks the fastest per fit-size bucket. Additions, no reference counterpart. */
+/* Loss-kernel variant (block size, occupancy target): -1 = automatic. All
+ * variants produce identical results; the autotuner times them at a fit's
+ * first Step and keeps the fastest per fit-size bucket (power of two of live
+ * targets). Additions, no reference counterpart. */
 int vm_set_loss_variant(vm_optimizer *h, int variant);
 int vm_get_loss_variant(vm_optimizer *h, int *variant, int *count);
 /* EvaluateLoss()  voro_optimizer.h:113 */
@@ -209,7 +210,9 @@ typedef struct {
     size_t hbmBudgetBytes;
     int maxLive;
     int stepsPerRound;
-    int lossVariant; /* -1 = default */
+    int lossVariant;       /* -1 = default */
+    size_t maxLiveTargets; /* admit while the live fits' targets stay within this (0 = no cap); a
+                              cap keeps the GPU busy while letting early requests finish sooner */
 } vms_config;
 typedef struct {
     double arrival, admitted, finished;
