@@ -49,3 +49,14 @@ struct PdParams {
 };
 cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int trials,
                                unsigned roundBase, cudaStream_t s);
+// One sampler's region resample for pd_launch_resample_many.
+struct PdJob {
+    float2 *grid;
+    PdParams p;
+    int x0, y0, x1, y1, trials;
+    unsigned roundBase;
+};
+// 1 when the region runs as one block (every phase in one pass of it).
+int pd_small_region(int x0, int y0, int x1, int y1);
+// Small regions of distinct samplers (jobs in device memory), one block each.
+cudaError_t pd_launch_resample_many(const PdJob *jobs, int n, cudaStream_t s);

@@ -88,8 +88,8 @@ __global__ void __launch_bounds__(256) k_phase(float2 *grid, PdParams p, int x0,
 // launches by one when every phase fits in one pass of the block.
 constexpr int kSmallBlock = 1024;
 
-__global__ void __launch_bounds__(kSmallBlock) k_resample_block(float2 *grid, PdParams p, int x0, int y0, int x1,
-                                                                 int y1, int trials, unsigned roundBase)
+__device__ __forceinline__ void resample_block(float2 *grid, const PdParams &p, int x0, int y0, int x1, int y1,
+                                               int trials, unsigned roundBase)
 {
     int rw = x1 - x0, n = rw * (y1 - y0);
     for (int t = threadIdx.x; t < n; t += blockDim.x)
@@ -106,6 +106,20 @@ __global__ void __launch_bounds__(kSmallBlock) k_resample_block(float2 *grid, Pd
                 __syncthreads(); // the next phase sees this phase's samples
             }
     }
+}
+
+__global__ void __launch_bounds__(kSmallBlock) k_resample_block(float2 *grid, PdParams p, int x0, int y0, int x1,
+                                                                 int y1, int trials, unsigned roundBase)
+{
+    resample_block(grid, p, x0, y0, x1, y1, trials, roundBase);
+}
+
+// Many samplers' small regions in one launch, one block each (the samplers'
+// grids are disjoint, so the blocks are independent).
+__global__ void __launch_bounds__(kSmallBlock) k_resample_many(const PdJob *__restrict__ jobs)
+{
+    PdJob j = jobs[blockIdx.x];
+    resample_block(j.grid, j.p, j.x0, j.y0, j.x1, j.y1, j.trials, j.roundBase);
 }
 
 } // namespace vmk
@@ -133,5 +147,18 @@ cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1,
         for (int py = 0; py < 3; ++py)
             for (int px = 0; px < 3; ++px) k_phase<<<pb, 256, 0, s>>>(grid, p, x0, y0, x1, y1, px, py, kx, ky);
     }
+    return cudaGetLastError();
+}
+
+int pd_small_region(int x0, int y0, int x1, int y1)
+{
+    long long phaseCells = (long long)((x1 - x0 + 2) / 3) * ((y1 - y0 + 2) / 3);
+    return x1 > x0 && y1 > y0 && phaseCells <= kSmallBlock;
+}
+
+cudaError_t pd_launch_resample_many(const PdJob *jobs, int n, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    k_resample_many<<<n, kSmallBlock, 0, s>>>(jobs);
     return cudaGetLastError();
 }

@@ -1157,6 +1157,68 @@ int pd_resample(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, float *gpuMs)
     return VM_OK;
 }
 
+int pd_resample_many(pd_sampler *const *samplers, const int *regions, int n, float *gpuMs)
+{
+    if (gpuMs) *gpuMs = 0.0f;
+    if (n < 0 || (n && (!samplers || !regions))) return fail(VM_ERR_ARG, "pd_resample_many: bad arguments");
+    for (int i = 0; i < n; ++i) {
+        if (!samplers[i]) return fail(VM_ERR_ARG, "pd_resample_many: NULL sampler");
+        for (int k = 0; k < i; ++k)
+            if (samplers[k] == samplers[i]) return fail(VM_ERR_ARG, "pd_resample_many: a sampler appears twice");
+    }
+    cudaError_t e;
+    std::vector<PdJob> jobs;
+    std::vector<int> jobOf;
+    float total = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        pd_sampler *s = samplers[i];
+        const int *r = regions + 4 * (size_t)i;
+        int x0 = std::max(r[0], 0), y0 = std::max(r[1], 0), x1 = std::min(r[2], s->gridW), y1 = std::min(r[3], s->gridH);
+        if (x0 >= x1 || y0 >= y1) continue;
+        if (!pd_small_region(x0, y0, x1, y1)) { // a large region: its own launches
+            float ms = 0.0f;
+            int rc = pd_resample(s, x0, y0, x1, y1, &ms);
+            if (rc) return rc;
+            total += ms;
+            continue;
+        }
+        if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(e, "pd_resample_many sync");
+        PdParams p{s->width, s->height, s->radius, s->cellSize, s->gridW, s->gridH, s->seed};
+        jobs.push_back(PdJob{s->grid.p, p, x0, y0, x1, y1, s->trials, s->roundBase});
+        jobOf.push_back(i);
+    }
+    if (!jobs.empty()) {
+        pd_sampler *s0 = samplers[jobOf[0]];
+        cudaStream_t st = s0->stream;
+        PdJob *dJobs = nullptr;
+        size_t bytes = sizeof(PdJob) * jobs.size();
+        if ((e = cudaMallocAsync((void **)&dJobs, bytes, st))) return cuda_fail(e, "pd_resample_many jobs");
+        if ((e = cudaMemcpyAsync(dJobs, jobs.data(), bytes, cudaMemcpyHostToDevice, st)) ||
+            (e = cudaEventRecord(s0->ev0, st)) || (e = pd_launch_resample_many(dJobs, (int)jobs.size(), st)) ||
+            (e = cudaEventRecord(s0->ev1, st))) {
+            cudaFreeAsync(dJobs, st);
+            return cuda_fail(e, "pd_resample_many");
+        }
+        for (size_t k = 0; k < jobs.size(); ++k) {
+            pd_sampler *s = samplers[jobOf[k]];
+            const PdJob &j = jobs[k];
+            s->roundBase += (unsigned)s->trials;
+            size_t pitch = (size_t)s->gridW * sizeof(float2), off = (size_t)j.y0 * s->gridW + j.x0;
+            if ((e = cudaMemcpy2DAsync(s->cells.data() + off, pitch, s->grid.p + off, pitch,
+                                       (j.x1 - j.x0) * sizeof(float2), j.y1 - j.y0, cudaMemcpyDeviceToHost, st)))
+                break;
+        }
+        cudaFreeAsync(dJobs, st);
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        if (e || (e = e2)) return cuda_fail(e, "pd_resample_many read");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, s0->ev0, s0->ev1);
+        total += ms;
+    }
+    if (gpuMs) *gpuMs = total;
+    return VM_OK;
+}
+
 int pd_info(pd_sampler *s, pd_info_t *out)
 {
     if (!s || !out) return fail(VM_ERR_ARG, "bad arguments");

@@ -6,6 +6,6 @@ include/vm_capi.h; this package only marshals numpy arrays to it. Importing
 it requires the library to be built (there is no CPU fallback).
 """
 from ._lib import LIB_PATH, VmError, load
-from .optimizer import OptimizerParams, Sampler, VoroMesh2D, VoroOptimizer
+from .optimizer import OptimizerParams, Sampler, VoroMesh2D, VoroOptimizer, resample_many
 
-__all__ = ["LIB_PATH", "VmError", "load", "OptimizerParams", "Sampler", "VoroMesh2D", "VoroOptimizer"]
+__all__ = ["LIB_PATH", "VmError", "load", "OptimizerParams", "Sampler", "VoroMesh2D", "VoroOptimizer", "resample_many"]

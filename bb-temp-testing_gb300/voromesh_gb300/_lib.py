@@ -92,6 +92,7 @@ SIGNATURES = {
     "pd_create": [F, F, F, I, C.c_uint, P],
     "pd_destroy": [P],
     "pd_resample": [P, I, I, I, I, P],
+    "pd_resample_many": [P, P, I, P],
     "pd_info": [P, P],
     "pd_cells": [P, P],
     "pd_verify": [P, I, I, I, I, P],

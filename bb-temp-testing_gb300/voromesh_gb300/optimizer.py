@@ -307,3 +307,15 @@ class Sampler:
     def GridW(self) -> int: return self.info().gridW
     def GridH(self) -> int: return self.info().gridH
     def Trials(self) -> int: return self.info().trials
+
+
+def resample_many(samplers, regions) -> float:
+    """Resample(*regions[i]) on each of the distinct `samplers` at once (small
+    regions as one block each of a single launch); returns GPU ms."""
+    lib = load()
+    n = len(samplers)
+    handles = (C.c_void_p * max(n, 1))(*[s._h for s in samplers])
+    r = np.ascontiguousarray(np.asarray(regions, np.int32).reshape(n, 4))
+    ms = C.c_float()
+    check(lib.pd_resample_many(handles, ptr(r), n, C.byref(ms)), "resample_many")
+    return ms.value

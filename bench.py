@@ -54,9 +54,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
-    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit"],
+    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit", "poisson"],
                     help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads; "
-                         "extract: the cell clipper; edit: the local-edit pipeline")
+                         "extract: the cell clipper; edit: the local-edit pipeline; poisson: the sampler")
     ap.add_argument("--fits", type=int, default=512)
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--requests", type=int, default=200)
@@ -396,6 +396,37 @@ def run_edit(args):
                       "data": "synthetic"}), flush=True)
 
 
+def run_poisson(args):
+    """Poisson sampler: the r=1e-3 fill of [0,2]^2 (samples/s), and 512 samplers
+    of the editor's size (1024^2 domain, r=24) each resampling an 11x11-cell
+    region, all in one call (one block per region) against one call each."""
+    import voromesh_gb300 as vm
+
+    s = vm.Sampler(2.0, 2.0, RADIUS, 30, 1)
+    fills = [s.ResampleAll() for _ in range(3)]
+    n_samples = s.Count()
+    s.close()
+    n = 512
+    samplers = [vm.Sampler(1024.0, 1024.0, 24.0, 30, 1 + k) for k in range(n)]
+    regions = [((k * 7) % 50, (k * 11) % 50, (k * 7) % 50 + 11, (k * 11) % 50 + 11) for k in range(n)]
+    vm.resample_many(samplers[:4], regions[:4])  # warm-up
+    t0 = time.perf_counter()
+    gpu_many = vm.resample_many(samplers, regions)
+    wall_many = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gpu_one = sum(sm.Resample(*reg) for sm, reg in zip(samplers, regions))
+    wall_one = time.perf_counter() - t0
+    for sm in samplers:
+        sm.close()
+    print(json.dumps({"metric": "samples/s, Poisson fill r=1e-3 on [0,2]^2", "unit": "samples/s",
+                      "value": n_samples / (min(fills) / 1e3), "fill_ms": min(fills), "samples": n_samples,
+                      "regions": {"count": n, "cells_each": 121, "batched_gpu_ms": gpu_many,
+                                  "batched_wall_ms": wall_many * 1e3, "one_by_one_gpu_ms": gpu_one,
+                                  "one_by_one_wall_ms": wall_one * 1e3,
+                                  "regions_per_s_batched": n / wall_many, "regions_per_s_one_by_one": n / wall_one},
+                      "data": "synthetic"}), flush=True)
+
+
 def run_serve(args):
     """Served stream: Poisson arrivals, generators log-uniform in [1k, 1M],
     8x targets from the ellipse-union or star shapes (coin flip), retire at
@@ -463,6 +494,9 @@ def main():
         return
     if args.workload == "edit":
         run_edit(args)
+        return
+    if args.workload == "poisson":
+        run_poisson(args)
         return
     import torch
 

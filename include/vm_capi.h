@@ -256,6 +256,11 @@ int pd_create(float width, float height, float radius, int trials, unsigned seed
 int pd_destroy(pd_sampler *s);
 /* Resample(cx0, cy0, cx1, cy1) -> GPU ms  poisson_disk.h:33 */
 int pd_resample(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, float *gpuMs);
+/* Resample(regions[4i..4i+3]) of n distinct samplers at once: each small
+ * region (every phase in one pass of a block) runs as one block of a single
+ * launch, larger ones as pd_resample. Same samples as n pd_resample calls.
+ * An addition, no reference counterpart. */
+int pd_resample_many(pd_sampler *const *samplers, const int *regions, int n, float *gpuMs);
 /* Width/Height/Radius/CellSize/GridW/GridH/Trials  poisson_disk.h:44-50 */
 int pd_info(pd_sampler *s, pd_info_t *out);
 /* Cells(): gridW*gridH (x,y) pairs, x < 0 = empty  poisson_disk.h:41 */

@@ -33,3 +33,21 @@ def test_region_resample_both_paths(vm, orc):
         assert s.Verify(*reg)
     cells, _ = orc.poisson_fill(2.0, 1.0, 0.013, 30, 5, regions)
     assert np.array_equal(s.Cells(), cells)
+
+
+def test_resample_many_equals_one_by_one(vm, orc):
+    """Many samplers' regions in one call (small regions as one block each of
+    a single launch, large ones on their own) give each sampler the samples of
+    its own Resample call."""
+    shapes = [(1.0, 1.0, 0.02, 30, 7), (2.0, 1.0, 0.013, 30, 8), (1.0, 1.0, 0.05, 20, 9), (0.5, 0.8, 0.01, 30, 10)]
+    regions = [(5, 5, 17, 13), (10, 10, 200, 100), (0, 0, 40, 40), (3, 2, 30, 20)]
+    many = [vm.Sampler(*sh) for sh in shapes]
+    vm.resample_many(many, regions)
+    for s, sh, reg in zip(many, shapes, regions):
+        cells, _ = orc.poisson_fill(sh[0], sh[1], sh[2], sh[3], sh[4], [reg])
+        assert np.array_equal(s.Cells(), cells)
+        assert s.Verify(*reg)
+        s.close()
+    with pytest.raises(vm.VmError):
+        s = vm.Sampler(1.0, 1.0, 0.02)
+        vm.resample_many([s, s], [(0, 0, 4, 4), (4, 4, 8, 8)])
