@@ -86,3 +86,23 @@ def test_serve_equals_alone(vm):
     one = serve(specs, arrivals, hbm_budget=1 << 30, max_live=1, steps_per_round=10, max_steps=40, rel_tol=0.0)
     for g1, g2 in zip(one.generators, r.generators):
         assert np.array_equal(g1, g2)
+
+
+def test_serve_target_cap(vm):
+    """A live-target cap changes when requests are admitted, not their results."""
+    from voromesh_gb300.batch import serve
+
+    specs = small_batch(6, seed=8)
+    arrivals = np.zeros(len(specs))
+    cap = max(len(s.targets) for s in specs) + 1
+    r = serve(specs, arrivals, hbm_budget=1 << 30, max_live=64, steps_per_round=10, max_steps=20, rel_tol=0.0,
+              max_live_targets=cap)
+    assert np.all(r.status == 0)
+    # with the cap, no two requests both larger than half of it ran together
+    big = [i for i, s in enumerate(specs) if len(s.targets) > cap // 2]
+    for a in big:
+        for b in big:
+            if a < b:
+                assert r.admitted[b] >= r.finished[a] or r.admitted[a] >= r.finished[b]
+    for spec, g in zip(specs, r.generators):
+        assert np.array_equal(g, alone(spec, 20))
