@@ -405,6 +405,7 @@ def run_poisson(args):
     s = vm.Sampler(2.0, 2.0, RADIUS, 30, 1)
     fills = [s.ResampleAll() for _ in range(3)]
     n_samples = s.Count()
+    s_info = (s.GridW(), s.GridH())
     s.close()
     n = 512
     samplers = [vm.Sampler(1024.0, 1024.0, 24.0, 30, 1 + k) for k in range(n)]
@@ -418,8 +419,13 @@ def run_poisson(args):
     wall_one = time.perf_counter() - t0
     for sm in samplers:
         sm.close()
+    peak, peak_kind = measured_peaks()
+    grid_cells = s_info[0] * s_info[1]
+    fill_gbs = 16 * grid_cells / (min(fills) / 1e3) / 1e9  # B_fill = 16 B per grid cell
     print(json.dumps({"metric": "samples/s, Poisson fill r=1e-3 on [0,2]^2", "unit": "samples/s",
                       "value": n_samples / (min(fills) / 1e3), "fill_ms": min(fills), "samples": n_samples,
+                      "roofline": {"bound": "hbm", "bytes_per_fill": 16 * grid_cells, "achieved": fill_gbs,
+                                   "unit": "GB/s", "peak": peak, "peak_kind": peak_kind, "frac": fill_gbs / peak},
                       "regions": {"count": n, "cells_each": 121, "batched_gpu_ms": gpu_many,
                                   "batched_wall_ms": wall_many * 1e3, "one_by_one_gpu_ms": gpu_one,
                                   "one_by_one_wall_ms": wall_one * 1e3,
@@ -543,6 +549,7 @@ def main():
     loss_ms = float(stages[0])
     lossBytes = 8 * N_TARGETS + 12 * N_SITES + 4 * (opt.info().gridW * opt.info().gridH + 1) + 16 * N_SITES
     peak, peak_kind = measured_peaks()
+    stepBytes = 88 * N_SITES + 8 * N_TARGETS + 8 * opt.info().gridW * opt.info().gridH
     achieved = lossBytes / (loss_ms / 1e3) / 1e9
     traffic = ncu_traffic()
     info = opt.info()
@@ -592,6 +599,9 @@ def main():
             "roofline": {"bound": "hbm", "kernel": "k_loss", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes_per_launch": lossBytes, "mean_launch_ms": loss_ms},
+            # the whole step against HBM: B_step = 88 B per site + 8 B per target + 8 B per cell
+            "step_roofline": {"bytes_per_step": stepBytes, "achieved": stepBytes / (ms / args.steps) / 1e6,
+                              "unit": "GB/s", "frac": stepBytes / (ms / args.steps) / 1e6 / peak},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": KERNELS_PER_STEP * args.steps,
