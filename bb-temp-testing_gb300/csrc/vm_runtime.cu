@@ -137,6 +137,7 @@ struct vm_optimizer {
     int lossVariant = 3;   // loss kernel variant in use
     int lossForced = -1;   // variant chosen by the caller (vm_set_loss_variant), -1 = automatic
     bool tunePending = false; // the autotuner still has to pick the variant
+    VmState *pinnedState = nullptr; // host staging of the state read after each Step
 
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -363,9 +364,12 @@ int ensure_graph(vm_optimizer *h)
 
 int read_state(vm_optimizer *h, VmState &st)
 {
-    cudaError_t e = cudaMemcpyAsync(&st, h->state.p, sizeof(VmState), cudaMemcpyDeviceToHost, h->stream);
+    // through a pinned staging copy: one direct DMA per Step
+    VmState *dst = h->pinnedState ? h->pinnedState : &st;
+    cudaError_t e = cudaMemcpyAsync(dst, h->state.p, sizeof(VmState), cudaMemcpyDeviceToHost, h->stream);
     if (!e) e = cudaStreamSynchronize(h->stream);
     if (e) return cuda_fail(e, "read state");
+    if (dst != &st) st = *dst;
     return VM_OK;
 }
 
@@ -522,6 +526,10 @@ int vm_create(float width, float height, float spacing, const vm_params *params,
     if (!rc && (e = vm_queue_init(h->queue.p, nullptr, 0, h->stream))) rc = cuda_fail(e, "queue");
     if (!rc && (e = cudaMemset(h->counts.p, 0, sizeof(int) * (h->cells + 1)))) rc = cuda_fail(e, "memset");
     if (!rc && (e = cudaMemset(h->state.p, 0, sizeof(VmState)))) rc = cuda_fail(e, "memset");
+    if (!rc && cudaMallocHost((void **)&h->pinnedState, sizeof(VmState)) != cudaSuccess) {
+        h->pinnedState = nullptr; // pageable reads still work
+        cudaGetLastError();
+    }
     if (!rc) h->lossGrid = vm_loss_occupancy_blocks(h->lossVariant);
     if (!rc) rc = upload_tables(h);
     if (rc) {
@@ -541,6 +549,7 @@ int vm_destroy(vm_optimizer *h)
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->pinnedState) cudaFreeHost(h->pinnedState);
     delete h; // DevBuf members free their memory
     return VM_OK;
 }
