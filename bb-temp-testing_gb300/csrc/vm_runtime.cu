@@ -240,10 +240,11 @@ void choose_loss_variant(vm_optimizer *h, int sms)
     set_loss_variant(h, v);
 }
 
-// The autotuner: per power-of-two bucket of live targets, the loss variant
-// with the shortest measured pass, kept for the process.
+// The autotuner: per device and power-of-two bucket of live targets, the loss
+// variant with the shortest measured pass, kept for the process.
 std::mutex g_tuneMu;
-int g_tuned[64];
+constexpr int kTuneDevices = 16;
+int g_tuned[kTuneDevices][64]; // [device][bucket] -> variant, -1 = not yet timed
 bool g_tunedInit = false;
 
 int tune_bucket(int live)
@@ -262,14 +263,18 @@ int autotune_loss_variant(vm_optimizer *h)
 {
     h->tunePending = false;
     int bucket = tune_bucket(h->liveTargets);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dev = std::min(std::max(dev, 0), kTuneDevices - 1); // devices past the table share its last row
     {
         std::lock_guard<std::mutex> lk(g_tuneMu);
         if (!g_tunedInit) {
-            for (int &t : g_tuned) t = -1;
+            for (auto &row : g_tuned)
+                for (int &t : row) t = -1;
             g_tunedInit = true;
         }
-        if (g_tuned[bucket] >= 0) {
-            set_loss_variant(h, g_tuned[bucket]);
+        if (g_tuned[dev][bucket] >= 0) {
+            set_loss_variant(h, g_tuned[dev][bucket]);
             return upload_tables(h);
         }
     }
@@ -304,7 +309,7 @@ int autotune_loss_variant(vm_optimizer *h)
         return cuda_fail(e, "tune restore");
     {
         std::lock_guard<std::mutex> lk(g_tuneMu);
-        g_tuned[bucket] = best;
+        g_tuned[dev][bucket] = best;
     }
     set_loss_variant(h, best);
     return upload_tables(h);
