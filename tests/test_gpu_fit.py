@@ -125,3 +125,20 @@ def test_loss_variants_and_target_order_agree(vm, orc, monkeypatch, sub):
         opt.SetGenerators(gen, len(gen), 1, 2.0)
         opt.Step(6)
         assert np.array_equal(opt.Generators(), g), f"variant {variant}"
+
+
+@pytest.mark.parametrize("jitter", [1e-6, 0.0])
+def test_lattice_fit_bit_exact(vm, orc, jitter):
+    """The precision-stress shape: a jittered (or exact) lattice of sites, where
+    bisector distances tie or nearly tie, so the staged path's exact fallbacks
+    and the deferred ring search both run; the trajectory equals the oracle's."""
+    from voromesh_gb300 import synth
+
+    gen = synth.lattice(3, 5, 64, 64, jitter)
+    tgt = synth.five_arm_star(3, 6, 40000)
+    opt, ref = _pair(vm, orc, gen, tgt, 2.0 / 64, 16, 0, 1.0)
+    for chunk in (1, 9):
+        opt.Step(chunk)
+        ref.step(chunk)
+        g, m, v = ref.generators()
+        assert np.array_equal(opt.Generators(), g)
