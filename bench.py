@@ -74,6 +74,18 @@ def dist_env():
     return world, rank, local
 
 
+def job_rate(ms: float, units: float, world: int, dist, device: str = "cpu"):
+    """Whole-job rate of `world` replicas that each processed `units` in `ms`:
+    the slowest rank's time (max over ranks) and units x world / that time."""
+    import torch
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return ms_max, units * world / (ms_max / 1e3)
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -538,11 +550,7 @@ def main():
     with ClockSampler(local) as clk:
         ms = opt.Step(args.steps)
     barrier()
-    ms_t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = N_SITES * args.steps * world / (ms / 1e3)
+    ms, value = job_rate(ms, N_SITES * args.steps, world, dist, "cuda")
 
     # ---- roofline of the loss kernel (stage events around each kernel)
     stages = opt.StepTimed(args.steps)
