@@ -256,7 +256,7 @@ int tune_bucket(int live)
 
 int read_state(vm_optimizer *h, VmState &st);
 
-// Times every variant on this fit (3 loss passes each, after one untimed
+// Times every variant on this fit (5 loss passes each, after one untimed
 // pass, in two sweeps) and keeps the fastest. The passes leave the generators and moments
 // alone; the gradient accumulators and the state are restored afterwards.
 int autotune_loss_variant(vm_optimizer *h)
@@ -290,7 +290,7 @@ int autotune_loss_variant(vm_optimizer *h)
             if ((rc = upload_tables(h))) return rc;
             int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
             float ms = 0.0f;
-            for (int k = 0; k < 4; ++k) {
+            for (int k = 0; k < 6; ++k) {
                 if (k == 1 && (e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "tune event");
                 if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, v, h->queue.p,
                                         h->stream)) ||
