@@ -65,4 +65,26 @@ struct MeshHost {
 // (mesh.cellStart, cellVerts, cellLabels, inside).
 void assemble_boundary(int n, MeshHost &mesh);
 
+// Device view of a canvas for the optimiser hand-off (vm_canvas.cu): its
+// target slots and occupancy, and the last edit's dirty slots, their values
+// and tile rectangle. Valid until the next canvas call.
+struct CanvasView {
+    const float2 *slots;
+    int nslots;
+    const unsigned long long *inside;
+    int tilesX, tilesY;
+    float voxelSize;
+    const int *dirty;
+    const float2 *dirtyValues;
+    int ndirty;
+    int tx0, ty0, tx1, ty1;
+    cudaStream_t stream;
+};
+int canvas_view(cv_canvas *c, CanvasView *v);
+// p[0..n) = {-1, -1} (empty slots)
+cudaError_t canvas_fill_empty(float2 *p, size_t n, cudaStream_t s);
+// dst[rect] = src[rect] for tile words of row pitch `pitch`
+cudaError_t canvas_copy_rect(const unsigned long long *src, unsigned long long *dst, int pitch, int tx0, int ty0,
+                             int tx1, int ty1, cudaStream_t s);
+
 } // namespace vmh

@@ -559,9 +559,8 @@ int vm_destroy(vm_optimizer *h)
     return VM_OK;
 }
 
-int vm_set_targets(vm_optimizer *h, const float *xy, int n)
+static int set_targets_from(vm_optimizer *h, const void *xy, int n, cudaMemcpyKind kind)
 {
-    if (!h || n < 0 || (n > 0 && !xy)) return fail(VM_ERR_ARG, "vm_set_targets: bad arguments");
     int cap = std::max(n, 1);
     int rc;
     if (cap != h->targetCapacity) {
@@ -574,10 +573,16 @@ int vm_set_targets(vm_optimizer *h, const float *xy, int n)
     cudaError_t e;
     // NaN padding fails every x >= 0 test (reference voro_optimizer.cu:558)
     if ((e = cudaMemsetAsync(h->traw.p, 0xFF, sizeof(float2) * cap, h->stream))) return cuda_fail(e, "memset targets");
-    if (n > 0 && (e = cudaMemcpyAsync(h->traw.p, xy, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, h->stream)))
+    if (n > 0 && (e = cudaMemcpyAsync(h->traw.p, xy, sizeof(float2) * (size_t)n, kind, h->stream)))
         return cuda_fail(e, "upload targets");
     if ((rc = upload_tables(h))) return rc;
     return sort_targets(h);
+}
+
+int vm_set_targets(vm_optimizer *h, const float *xy, int n)
+{
+    if (!h || n < 0 || (n > 0 && !xy)) return fail(VM_ERR_ARG, "vm_set_targets: bad arguments");
+    return set_targets_from(h, xy, n, cudaMemcpyHostToDevice);
 }
 
 int vm_update_targets(vm_optimizer *h, const int *dirty, int ndirty, const float *slots, int nslots)
@@ -1077,6 +1082,70 @@ int vm_mesh_copy(vm_optimizer *h, float *generators, uint8_t *inside, int *cellS
     if (vertices) std::memcpy(vertices, M.vertices.data(), sizeof(float2) * M.vertices.size());
     if (edges) std::memcpy(edges, M.edges.data(), sizeof(int) * M.edges.size());
     if (cellLabels) std::memcpy(cellLabels, M.cellLabels.data(), sizeof(int) * M.cellLabels.size());
+    return VM_OK;
+}
+
+// ===========================================================================
+// canvas hand-off (device to device)
+// ===========================================================================
+int vm_set_targets_from_canvas(vm_optimizer *h, cv_canvas *c)
+{
+    if (!h || !c) return fail(VM_ERR_ARG, "vm_set_targets_from_canvas: NULL handle");
+    CanvasView v{};
+    int rc;
+    if ((rc = canvas_view(c, &v))) return rc;
+    // SetTargets(canvas.TargetSlots()) (voro_optimizer.cu:549-560)
+    if ((rc = set_targets_from(h, v.slots, v.nslots, cudaMemcpyDeviceToDevice))) return rc;
+    // SetOccupancy(InsideMasks(), TilesX(), TilesY(), VoxelSize()) (:589-600)
+    size_t n = (size_t)v.tilesX * v.tilesY;
+    if (v.tilesX != h->tilesX || v.tilesY != h->tilesY) {
+        h->tilesX = v.tilesX;
+        h->tilesY = v.tilesY;
+        if ((rc = h->occ.alloc(n))) return rc;
+    }
+    h->invVoxel = 1.0f / v.voxelSize;
+    cudaError_t e;
+    if (n && (e = cudaMemcpyAsync(h->occ.p, v.inside, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, h->stream)))
+        return cuda_fail(e, "canvas occupancy");
+    if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "canvas occupancy");
+    return VM_OK;
+}
+
+int vm_update_from_canvas(vm_optimizer *h, cv_canvas *c)
+{
+    if (!h || !c) return fail(VM_ERR_ARG, "vm_update_from_canvas: NULL handle");
+    CanvasView v{};
+    int rc;
+    cudaError_t e;
+    if ((rc = canvas_view(c, &v))) return rc;
+    // UpdateTargets(edit.dirtySlots, TargetSlots()) (voro_optimizer.cu:562-587)
+    if (v.ndirty > 0) {
+        if (v.nslots > h->targetCapacity) {
+            // grow with slack: the slot array, then {-1, -1} slots (:566-571)
+            size_t cap = std::max((size_t)v.nslots * 3 / 2, (size_t)v.nslots + 64);
+            drop_graph(h);
+            h->targetCapacity = (int)cap;
+            if ((rc = h->traw.alloc(cap)) || (rc = h->tkey.alloc(cap)) || (rc = h->trank.alloc(cap)) ||
+                (rc = h->tpos.alloc(cap)) || (rc = h->tslot.alloc(cap)))
+                return rc;
+            if ((e = cudaMemcpyAsync(h->traw.p, v.slots, sizeof(float2) * (size_t)v.nslots, cudaMemcpyDeviceToDevice,
+                                     h->stream)) ||
+                (e = canvas_fill_empty(h->traw.p + v.nslots, cap - (size_t)v.nslots, h->stream)))
+                return cuda_fail(e, "canvas targets");
+            if ((rc = upload_tables(h))) return rc;
+        } else if ((e = vm_launch_scatter_targets(h->traw.p, v.dirty, v.dirtyValues, v.ndirty, h->stream))) {
+            return cuda_fail(e, "canvas targets");
+        }
+        if ((rc = sort_targets(h))) return rc;
+    }
+    // UpdateOccupancy(InsideMasks(), edit tile rectangle) (:602-611)
+    if (v.tilesX != h->tilesX || v.tilesY != h->tilesY)
+        return fail(VM_ERR_STATE, "vm_update_from_canvas: occupancy grid differs from the canvas (SetOccupancy first)");
+    int tx0 = std::max(v.tx0, 0), ty0 = std::max(v.ty0, 0);
+    int tx1 = std::min(v.tx1, h->tilesX), ty1 = std::min(v.ty1, h->tilesY);
+    if ((e = canvas_copy_rect(v.inside, h->occ.p, h->tilesX, tx0, ty0, tx1, ty1, h->stream)) ||
+        (e = cudaStreamSynchronize(h->stream)))
+        return cuda_fail(e, "canvas occupancy");
     return VM_OK;
 }
 

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 
+#include "gb300_access.h"
 #include "vm_capi.h"
 
 static_assert(sizeof(voromesh::Vec2) == 2 * sizeof(float), "Vec2 must mirror float2");
@@ -159,6 +160,15 @@ VoroMesh2D VoroOptimizer::Extract()
     mesh.gpuMs = info.gpuMs;
     mesh.hostMs = info.hostMs;
     return mesh;
+}
+
+vm_optimizer *Gb300Access::handle(VoroOptimizer &opt) { return opt.mDev->h; }
+
+void Gb300Access::refresh(VoroOptimizer &opt)
+{
+    vm_info_t info;
+    check(vm_info(opt.mDev->h, &info), "VoroOptimizer");
+    opt.mTargetCapacity = info.targetCapacity;
 }
 
 // The step graph, grid build and iteration are enqueued inside the library;

@@ -50,6 +50,17 @@ class vm_mesh_info(C.Structure):
                 ("overflowCells", C.c_int), ("gpuMs", C.c_float), ("hostMs", C.c_float)]
 
 
+class cv_edit(C.Structure):
+    _fields_ = [("tx0", C.c_int), ("ty0", C.c_int), ("tx1", C.c_int), ("ty1", C.c_int), ("removed", C.c_int),
+                ("added", C.c_int), ("flipped", C.c_int), ("ndirty", C.c_int)]
+
+
+class cv_info_t(C.Structure):
+    _fields_ = [("voxelsX", C.c_int), ("voxelsY", C.c_int), ("tilesX", C.c_int), ("tilesY", C.c_int),
+                ("voxelSize", C.c_float), ("numSlots", C.c_int), ("freeSlots", C.c_int),
+                ("surfaceCount", C.c_longlong), ("surfaceTiles", C.c_int)]
+
+
 class pd_info_t(C.Structure):
     _fields_ = [("width", C.c_float), ("height", C.c_float), ("radius", C.c_float), ("cellSize", C.c_float),
                 ("gridW", C.c_int), ("gridH", C.c_int), ("trials", C.c_int), ("seed", C.c_uint),
@@ -97,6 +108,21 @@ SIGNATURES = {
     "pd_cells": [P, P],
     "pd_verify": [P, I, I, I, I, P],
     "pd_count": [P, P],
+    "cv_create": [F, F, F, P],
+    "cv_destroy": [P],
+    "cv_rasterize": [P, P, I, P],
+    "cv_stamp_disc": [P, F, F, F, I, P],
+    "cv_edit_dirty": [P, P, P, I],
+    "cv_info": [P, P],
+    "cv_get_slots": [P, P],
+    "cv_get_inside": [P, P],
+    "cv_get_inside_rect": [P, P, I, I, I, I],
+    "cv_get_surface": [P, P, P, P],
+    "cv_get_free": [P, P],
+    "cv_is_inside": [P, I, I, P],
+    "cv_is_surface": [P, I, I, P],
+    "vm_set_targets_from_canvas": [P, P],
+    "vm_update_from_canvas": [P, P],
     # seeded generators (host only)
     "vm_synth_uniform": [C.c_uint64, C.c_uint64, C.c_int64, C.c_double, C.c_double, I, P],
     "vm_synth_circle": [C.c_uint64, C.c_uint64, C.c_int64, C.c_double, C.c_double, I, P],

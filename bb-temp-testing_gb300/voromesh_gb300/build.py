@@ -28,8 +28,9 @@ NVFLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler"
                   "-I" + str(INCLUDE), "-I" + str(CSRC)]
 CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11"]
 
-CU_SOURCES = ["vm_loss.cu", "vm_step.cu", "vm_extract.cu", "vm_poisson.cu", "vm_runtime.cu", "vm_batch.cu", "vm_noalloc.cu"]
-CXX_SOURCES = ["voro_optimizer.cpp", "poisson_disk.cpp"]
+CU_SOURCES = ["vm_loss.cu", "vm_step.cu", "vm_extract.cu", "vm_poisson.cu", "vm_canvas.cu", "vm_runtime.cu", "vm_batch.cu",
+              "vm_noalloc.cu"]
+CXX_SOURCES = ["voro_optimizer.cpp", "poisson_disk.cpp", "canvas.cpp"]
 C_SOURCES = ["synth.c"]
 
 

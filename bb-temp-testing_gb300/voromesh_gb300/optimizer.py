@@ -115,6 +115,15 @@ class VoroOptimizer:
         m = np.ascontiguousarray(masks, dtype=np.uint64)
         check(self._lib.vm_update_occupancy(self._h, ptr(m), tx0, ty0, tx1, ty1), "UpdateOccupancy")
 
+    # ---- device-to-device hand-off from a Canvas (GB300 extension) ----
+    def SetTargetsFromCanvas(self, canvas) -> None:
+        """SetTargets(canvas.TargetSlots()) + SetOccupancy(canvas.InsideMasks(), ...) without a host copy."""
+        check(self._lib.vm_set_targets_from_canvas(self._h, canvas._h), "SetTargetsFromCanvas")
+
+    def UpdateFromCanvas(self, canvas) -> None:
+        """UpdateTargets + UpdateOccupancy for the canvas's last edit, device to device."""
+        check(self._lib.vm_update_from_canvas(self._h, canvas._h), "UpdateFromCanvas")
+
     def SetGenerators(self, slots, slotsW: int, slotsH: int, slotCellSize: float) -> None:
         a = _pts(slots, "slots")
         if len(a) != slotsW * slotsH:

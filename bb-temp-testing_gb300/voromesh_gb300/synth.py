@@ -178,3 +178,29 @@ def arrival_times(seed: int, n: int, rate: float) -> np.ndarray:
     u = uniform01(seed, 13, n)
     gaps = np.array([-lib.vm_synth_log(1.0 - x) / rate for x in u])
     return np.cumsum(gaps)
+
+
+def heart(cx: float, cy: float, width: float, segments: int) -> np.ndarray:
+    """Closed polygon of the parametric heart x = 16 sin^3 t, y = 13 cos t -
+    5 cos 2t - 2 cos 3t - cos 4t, `width` wide, centred on (cx, cy), y down
+    (the outline of the reference's editor demo, include/voromesh/shape2d.h:21).
+    Evaluated in float64 and rounded to float32."""
+    t = 2.0 * np.pi * np.arange(segments) / segments
+    s = np.sin(t)
+    x = 16.0 * s ** 3
+    y = 13.0 * np.cos(t) - 5.0 * np.cos(2 * t) - 2.0 * np.cos(3 * t) - np.cos(4 * t)
+    scale = width / 32.0
+    return np.stack([cx + scale * x, cy - scale * (y + 2.5)], 1).astype(np.float32)
+
+
+def comb(x0: float, y0: float, width: float, height: float, teeth: int) -> np.ndarray:
+    """Closed comb polygon: `teeth` vertical teeth over [x0, x0 + width],
+    joined at the bottom; every scanline through the teeth crosses 2 * teeth
+    edges."""
+    pts = []
+    w = width / (2 * teeth)
+    for k in range(teeth):
+        xa, xb = x0 + 2 * k * w, x0 + (2 * k + 1) * w
+        pts += [(xa, y0 + height), (xa, y0), (xb, y0), (xb, y0 + height)]
+    pts += [(x0 + width, y0 + height), (x0 + width, y0 + height * 1.1), (x0, y0 + height * 1.1)]
+    return np.asarray(pts, np.float32)

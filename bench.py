@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
-    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit", "poisson"],
+    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit", "poisson", "canvas"],
                     help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads; "
                          "extract: the cell clipper; edit: the local-edit pipeline; poisson: the sampler")
     ap.add_argument("--fits", type=int, default=512)
@@ -336,74 +336,40 @@ def run_extract(args):
 def run_edit(args):
     """The local-edit pipeline of the reference's editor (Editor::Stamp,
     apps/voromesh_demo.cpp:117-156) with its defaults: a 1024 x 1024 domain,
-    1-unit voxels, Poisson radius 24 (61 x 61 generator slots), 100 local
-    steps, sample fraction 0.2. The canvas is a stand-in: the object is a
-    union of discs, its surface targets lie on the outline at unit spacing,
-    and each edit adds a disc of radius 40 on the outline. Each stamp runs
-    UpdateTargets + UpdateOccupancy, a region Resample + UpdateGenerators,
-    BeginSchedule on the region + Optimize, and Extract; wall ms per phase."""
+    1-unit voxels, the heart outline (4096 segments), Poisson radius 24 (61 x 61
+    generator slots), brush radius 48, 100 local steps, sample fraction 0.2.
+    The canvas is the device Canvas; each stamp runs StampDisc, the
+    UpdateTargets + UpdateOccupancy hand-off (device to device), a region
+    Resample + UpdateGenerators, BeginSchedule on the region + Optimize, and
+    Extract; wall ms per phase. Stamps alternate add and carve along the
+    outline."""
     import voromesh_gb300 as vm
+    from voromesh_gb300 import synth
 
-    domain, voxel, radius, brush = 1024.0, 1.0, 24.0, 40.0
-    discs = [(512.0, 512.0, 300.0)]
-
-    def inside(x, y):
-        r = np.zeros(np.broadcast(x, y).shape, bool)
-        for cx, cy, rr in discs:
-            r |= (x - cx) ** 2 + (y - cy) ** 2 < rr * rr
-        return r
-
-    def rim(cx, cy, rr):
-        n = int(np.ceil(2 * np.pi * rr))
-        t = np.arange(n) * (2 * np.pi / n)
-        return np.stack([cx + rr * np.cos(t), cy + rr * np.sin(t)], 1).astype(np.float32)
-
-    nv = int(domain / voxel)
-    tiles = nv // 8
-    vc = (np.arange(nv) + 0.5) * voxel
-
-    def masks_of():
-        ins = inside(vc[None, :], vc[:, None])  # [y, x]
-        bits = ins.reshape(tiles, 8, tiles, 8).transpose(0, 2, 1, 3).reshape(tiles, tiles, 64).astype(np.uint64)
-        return (bits << np.arange(64, dtype=np.uint64)).sum(axis=2, dtype=np.uint64).reshape(-1)
-
-    slots = rim(*discs[0])
+    domain, voxel, radius = 1024.0, 1.0, 24.0
+    brush = 2.0 * radius
+    poly = synth.heart(0.5 * domain, 0.5 * domain, 0.8 * domain, 4096)
     params = vm.OptimizerParams()  # iterations 400, localIterations 100, sampleFraction 0.2
+    canvas = vm.Canvas(domain, domain, voxel)
     opt = vm.VoroOptimizer(domain, domain, radius, params)
     t0 = time.perf_counter()
-    opt.SetTargets(slots)
-    masks = masks_of()
-    opt.SetOccupancy(masks, tiles, tiles, voxel)
+    canvas.RasterizeShape(poly)
+    opt.SetTargetsFromCanvas(canvas)
     sampler = vm.Sampler(domain, domain, radius, 30, 1)
     opt.SetGenerators(sampler.Cells(), sampler.GridW(), sampler.GridH(), sampler.CellSize())
     global_gpu = opt.Optimize()
     opt.Extract()
     reset_ms = (time.perf_counter() - t0) * 1e3
     rows = []
-    n_stamps = 21
+    n_stamps = 33
     for k in range(n_stamps):
-        th = 2 * np.pi * k / n_stamps
-        cx, cy = 512.0 + 300.0 * np.cos(th), 512.0 + 300.0 * np.sin(th)
+        cx, cy = (float(v) for v in poly[(k * 4096) // n_stamps])
         ta = time.perf_counter()
-        # canvas stand-in: drop targets inside the new disc, add its rim outside the object
-        live = slots[:, 0] >= 0
-        gone = live & ((slots[:, 0] - cx) ** 2 + (slots[:, 1] - cy) ** 2 < brush * brush)
-        new = rim(cx, cy, brush)
-        new = new[~inside(new[:, 0], new[:, 1])]
-        discs.append((cx, cy, brush))
-        slots[gone] = -1.0
-        free = np.flatnonzero(slots[:, 0] < 0)
-        if len(free) < len(new):
-            slots = np.concatenate([slots, np.full((len(new) - len(free), 2), -1.0, np.float32)])
-            free = np.flatnonzero(slots[:, 0] < 0)
-        slots[free[:len(new)]] = new
-        dirty = np.concatenate([np.flatnonzero(gone), free[:len(new)]]).astype(np.int32)
-        masks = masks_of()
-        tx0, ty0 = int((cx - brush) // (8 * voxel)), int((cy - brush) // (8 * voxel))
-        tx1, ty1 = int(np.ceil((cx + brush) / (8 * voxel))), int(np.ceil((cy + brush) / (8 * voxel)))
+        e = canvas.StampDisc((cx, cy), brush, bool(k % 2 == 0), with_dirty=False)
         tb = time.perf_counter()
-        opt.UpdateTargets(dirty, slots)
-        opt.UpdateOccupancy(masks, max(tx0, 0), max(ty0, 0), min(tx1, tiles), min(ty1, tiles))
+        if not e.Changed():
+            continue
+        opt.UpdateFromCanvas(canvas)
         tc = time.perf_counter()
         margin, cs = brush + 2 * radius, sampler.CellSize()
         rx0, ry0 = max(int(np.floor((cx - margin) / cs)), 0), max(int(np.floor((cy - margin) / cs)), 0)
@@ -419,19 +385,93 @@ def run_edit(args):
         tf = time.perf_counter()
         if k:  # the first stamp warms up
             rows.append({"canvas": (tb - ta) * 1e3, "upload": (tc - tb) * 1e3, "poisson": (td - tc) * 1e3,
-                         "optimize": (te - td) * 1e3, "extract": (tf - te) * 1e3, "total_pipeline": (tf - tb) * 1e3,
+                         "optimize": (te - td) * 1e3, "extract": (tf - te) * 1e3, "total_pipeline": (tf - ta) * 1e3,
                          "poisson_gpu": pgpu, "optimize_gpu": ogpu, "extract_gpu": mesh.gpuMs,
-                         "slots": (rx1 - rx0) * (ry1 - ry0)})
+                         "removed": e.removed, "added": e.added, "slots": (rx1 - rx0) * (ry1 - ry0)})
     sampler.close()
     opt.close()
+    canvas.close()
     med = {key: float(np.median([r[key] for r in rows])) for key in rows[0]}
     print(json.dumps({"metric": "ms per local edit (p50), Editor::Stamp pipeline", "unit": "ms",
                       "value": med["total_pipeline"], "higher_is_better": False,
-                      "workload": "1024^2 domain, 1-unit voxels, Poisson r=24 (61x61 slots), 100 local steps, "
-                                  "sampleFraction 0.2, disc-union canvas stand-in, brush radius 40",
+                      "workload": "1024^2 domain, 1-unit voxels, heart outline (4096 segments), Poisson r=24 "
+                                  "(61x61 slots), 100 local steps, sampleFraction 0.2, device Canvas, brush radius 48",
                       "p50_ms": med, "p99_total_ms": float(np.percentile([r["total_pipeline"] for r in rows], 99)),
                       "stamps": len(rows), "reset_and_global_fit_ms": reset_ms, "global_fit_gpu_ms": global_gpu,
                       "data": "synthetic"}), flush=True)
+
+
+def run_canvas(args):
+    """Canvas (voromesh::Canvas, src/voromesh/canvas.cpp) on the GPU:
+    RasterizeShape of the editor's heart (1024^2 voxels, 4096 segments) and of
+    a fine outline (8192^2 voxels on the same domain, 65536 segments), then
+    brush stamps (radius 48 units, alternating add and carve along the
+    outline). Device ms and wall ms through the Python API against the CPU
+    oracle (the reference's Canvas is host code), with a bit-exact check of
+    the device state against the oracle's after each case."""
+    import voromesh_gb300 as vm
+    from voromesh_gb300 import synth
+    from oracle import oracle as orc
+
+    out = {}
+    peak, peak_kind = measured_peaks()
+    for name, V, segs, n_stamps in (("editor_1k", 1024, 4096, 64), ("fine_8k", 8192, 65536, 32)):
+        vs = 1024.0 / V
+        poly = synth.heart(512.0, 512.0, 819.2, segs)
+        c = vm.Canvas(1024.0, 1024.0, vs)
+        c.RasterizeShape(poly)
+        gpu, wall = [], []
+        for _ in range(max(args.warmup, 3)):
+            t0 = time.perf_counter()
+            gpu.append(c.RasterizeShape(poly))
+            wall.append((time.perf_counter() - t0) * 1e3)
+        o = orc.Canvas(1024.0, 1024.0, vs)
+        t0 = time.perf_counter()
+        o.rasterize(poly)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        inf = c.info()
+        raster_ok = np.array_equal(c.InsideMasks(), o.inside()) and \
+            np.array_equal(c.TargetSlots().view(np.uint32), o.slots().view(np.uint32))
+        # stamps
+        pts = [tuple(float(v) for v in poly[(k * segs) // n_stamps]) for k in range(n_stamps)]
+        sg, sw, so = [], [], []
+        for k, (cx, cy) in enumerate(pts):
+            t0 = time.perf_counter()
+            e = c.StampDisc((cx, cy), 48.0, k % 2 == 0)
+            sw.append((time.perf_counter() - t0) * 1e3)
+            t0 = time.perf_counter()
+            eo = o.stamp(cx, cy, 48.0, k % 2 == 0)
+            so.append((time.perf_counter() - t0) * 1e3)
+            raster_ok = raster_ok and np.array_equal(e.dirtySlots, eo.dirty)
+        st_ok = np.array_equal(c.TargetSlots().view(np.uint32), o.slots().view(np.uint32)) and \
+            np.array_equal(c.InsideMasks(), o.inside())
+        if V <= 2048:
+            try:
+                pi = orc.canvas_relabelling(c.state(), o.state())
+                st_ok = st_ok and bool(np.array_equal(pi, np.arange(len(pi))))
+            except AssertionError:
+                st_ok = False
+        out[name] = {"voxels": V * V, "segments": segs, "surface_voxels": int(inf.surfaceCount),
+                     "rasterize_gpu_ms": float(np.median(gpu)), "rasterize_wall_ms": float(np.median(wall)),
+                     "rasterize_cpu_oracle_ms": cpu_ms,
+                     "stamp_wall_ms_p50": float(np.median(sw[1:])), "stamp_cpu_oracle_ms_p50": float(np.median(so[1:])),
+                     "stamps": n_stamps, "bit_exact_vs_oracle": bool(raster_ok and st_ok)}
+        c.close()
+    f = out["fine_8k"]
+    vox_s = f["voxels"] / (f["rasterize_gpu_ms"] / 1e3)
+    # algorithmic bytes of one rasterisation: occupancy and surface masks
+    # written (2 x V^2 / 8 B), the surface points and slots of the surface
+    # voxels (12 B each) and their slots (8 B)
+    alg = 2 * f["voxels"] / 8 + 20 * f["surface_voxels"]
+    gbs = alg / (f["rasterize_gpu_ms"] / 1e3) / 1e9
+    print(json.dumps({"metric": "voxels/s, Canvas::RasterizeShape (8192^2 voxels, 65536-segment outline)",
+                      "unit": "voxels/s", "value": vox_s, "higher_is_better": True,
+                      "cpu_baseline": {"value": f["voxels"] / (f["rasterize_cpu_oracle_ms"] / 1e3), "unit": "voxels/s",
+                                       "cores": 1, "kind": "port",
+                                       "sample": "one RasterizeShape of the same outline by the oracle (1 thread)"},
+                      "roofline": {"bound": "hbm", "bytes_per_call": alg, "achieved": gbs, "unit": "GB/s",
+                                   "peak": peak, "peak_kind": peak_kind, "frac": gbs / peak},
+                      "cases": out, "data": "synthetic"}), flush=True)
 
 
 def run_poisson(args):
@@ -541,6 +581,9 @@ def main():
         return
     if args.workload == "poisson":
         run_poisson(args)
+        return
+    if args.workload == "canvas":
+        run_canvas(args)
         return
     import torch
 

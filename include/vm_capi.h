@@ -270,6 +270,75 @@ int pd_verify(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, int *ok);
 /* Number of samples in the grid. */
 int pd_count(pd_sampler *s, long long *n);
 
+/* --------------------------------------------------------------------------
+ * Canvas: the authoritative 2D shape, device-resident (voromesh::Canvas,
+ * include/voromesh/canvas.h:25-89, src/voromesh/canvas.cpp). Voxel (i, j)
+ * covers [i, i+1) x [j, j+1) * voxelSize; 8x8 voxels form a tile and voxel
+ * (i, j) is bit (j & 7) * 8 + (i & 7) of its tile's word. Occupancy is a dense
+ * row-major array of tile words; the surface (one mean boundary point and one
+ * target slot per surface voxel) is dense per voxel on the device. The target
+ * slot array (TargetSlots) lives on the device; {-1, -1} marks a free slot.
+ *
+ * Results equal the reference's Canvas on the same inputs, with one stated
+ * difference: a stamp's new rim voxels take their slots from the free list in
+ * tile-major voxel order, where the reference uses std::unordered_map order
+ * (canvas.cpp:200). Slot indices can therefore differ by a relabelling; every
+ * value, mask, point and count is the same.
+ * ------------------------------------------------------------------------ */
+typedef struct cv_canvas cv_canvas;
+
+typedef struct {
+    int tx0, ty0, tx1, ty1;     /* occupancy tiles [tx0,tx1) x [ty0,ty1) rewritten */
+    int removed, added, flipped; /* surface samples, occupancy voxels */
+    int ndirty;                 /* target slots whose value changed (cv_edit_dirty) */
+} cv_edit;
+
+typedef struct {
+    int voxelsX, voxelsY, tilesX, tilesY;
+    float voxelSize;
+    int numSlots, freeSlots;   /* TargetSlots().size(); free-list length */
+    long long surfaceCount;    /* Canvas::SurfaceCount */
+    int surfaceTiles;          /* Canvas::SurfaceTileCount */
+} cv_info_t;
+
+/* Canvas(width, height, voxelSize) (canvas.cpp:33-38) */
+int cv_create(float width, float height, float voxelSize, cv_canvas **out);
+int cv_destroy(cv_canvas *c);
+/* RasterizeShape(polygon) (canvas.cpp:71-134); n vertices (x, y), closed
+ * implicitly. gpuMs (optional) = device time of the call. At most 131072
+ * voxels per row and 32768 edge crossings on one scanline. */
+int cv_rasterize(cv_canvas *c, const float *xy, int n, float *gpuMs);
+/* StampDisc(center, radius, inside) (canvas.cpp:136-221) */
+int cv_stamp_disc(cv_canvas *c, float cx, float cy, float radius, int inside, cv_edit *out);
+/* The last edit's dirty slots (Edit::dirtySlots) and their new values
+ * (x, y pairs; may be NULL); cap = room in the buffers. */
+int cv_edit_dirty(cv_canvas *c, int *dirty, float *values, int cap);
+int cv_info(cv_canvas *c, cv_info_t *out);
+/* TargetSlots(): numSlots (x, y) pairs */
+int cv_get_slots(cv_canvas *c, float *xy);
+/* InsideMasks(): tilesX * tilesY words */
+int cv_get_inside(cv_canvas *c, uint64_t *masks);
+/* The words of tiles [tx0,tx1) x [ty0,ty1) only, into a tilesX * tilesY array */
+int cv_get_inside_rect(cv_canvas *c, uint64_t *masks, int tx0, int ty0, int tx1, int ty1);
+/* Dense surface state (each may be NULL): per tile its surface mask; per voxel
+ * (tile-major, 64 per tile) its point and slot, (-1, -1) / -1 off the surface. */
+int cv_get_surface(cv_canvas *c, uint64_t *masks, float *points, int *slots);
+/* The free list, bottom to top (freeSlots entries) */
+int cv_get_free(cv_canvas *c, int *freeList);
+/* IsInside(i, j) / IsSurface(i, j) (canvas.cpp:40-49) */
+int cv_is_inside(cv_canvas *c, int i, int j, int *out);
+int cv_is_surface(cv_canvas *c, int i, int j, int *out);
+
+/* Device-to-device hand-off from a canvas to an optimiser on the same GPU:
+ *   vm_set_targets_from_canvas = SetTargets(TargetSlots()) followed by
+ *     SetOccupancy(InsideMasks(), TilesX(), TilesY(), VoxelSize());
+ *   vm_update_from_canvas = UpdateTargets(edit.dirtySlots, TargetSlots())
+ *     followed by UpdateOccupancy(InsideMasks(), edit tile rectangle) for the
+ *     canvas's last edit (the editor's sequence, apps/voromesh_demo.cpp:124-125).
+ * No data passes through the host. */
+int vm_set_targets_from_canvas(vm_optimizer *h, cv_canvas *c);
+int vm_update_from_canvas(vm_optimizer *h, cv_canvas *c);
+
 #ifdef __cplusplus
 }
 #endif

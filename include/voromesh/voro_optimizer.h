@@ -100,6 +100,7 @@ public:
 
 private:
     struct Device;
+    friend struct Gb300Access; // canvas hand-off (gb300_ext.h); no effect on the layout
 
     void BuildGraph();
     void EnqueueBuildGrid();

@@ -340,3 +340,200 @@ def poisson_fill(width, height, radius, trials=30, seed=1, regions=()):
 
 def poisson_verify(p: VoPoisson, grid, x0, y0, x1, y1) -> bool:
     return bool(lib().vo_poisson_verify(C.byref(p), P(np.ascontiguousarray(grid, np.float32)), x0, y0, x1, y1))
+
+
+# ---------------------------------------------------------------------------
+# Canvas (src/voromesh/canvas.cpp): the oracle restatement (vo_canvas.c) and,
+# where it was built here, the reference's own class (oracle/_ref).
+# ---------------------------------------------------------------------------
+REF_CANVAS_LIB = HERE / "_ref" / "libref_canvas.so"
+_refc = None
+
+
+def ref_canvas_available() -> bool:
+    return REF_CANVAS_LIB.exists()
+
+
+def _canvas_lib() -> C.CDLL:
+    L = lib()
+    if not hasattr(L, "_canvas_ready"):
+        L.vo_canvas_create.restype = C.c_void_p
+        L.vo_canvas_create.argtypes = [C.c_float, C.c_float, C.c_float]
+        L.vo_canvas_destroy.argtypes = [C.c_void_p]
+        L.vo_canvas_rasterize.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        L.vo_canvas_stamp.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]
+        L.vo_canvas_dims.argtypes = [C.c_void_p, C.c_void_p]
+        L.vo_canvas_counts.argtypes = [C.c_void_p, C.c_void_p]
+        L.vo_canvas_get.argtypes = [C.c_void_p] + [C.c_void_p] * 7
+        L._canvas_ready = True
+    return L
+
+
+def ref_canvas() -> C.CDLL:
+    global _refc
+    if _refc is None:
+        _refc = C.CDLL(str(REF_CANVAS_LIB))
+        _refc.rc_canvas_create.restype = C.c_void_p
+        _refc.rc_canvas_create.argtypes = [C.c_float, C.c_float, C.c_float]
+        _refc.rc_canvas_destroy.argtypes = [C.c_void_p]
+        _refc.rc_canvas_rasterize.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        _refc.rc_canvas_stamp.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p,
+                                          C.c_void_p, C.c_int]
+        _refc.rc_canvas_counts.argtypes = [C.c_void_p, C.c_void_p]
+        _refc.rc_canvas_get.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+        _refc.rc_make_heart.argtypes = [C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]
+    return _refc
+
+
+def canvas_dims(width: float, height: float, voxel: float):
+    """voxelsX, voxelsY, tilesX, tilesY (canvas.cpp:33-38)."""
+    f = np.float32
+    vx = int(np.ceil(f(width) / f(voxel)))
+    vy = int(np.ceil(f(height) / f(voxel)))
+    return vx, vy, (vx + 7) // 8, (vy + 7) // 8
+
+
+class CanvasEdit:
+    def __init__(self, tx0=0, ty0=0, tx1=0, ty1=0, removed=0, added=0, flipped=0, dirty=()):
+        self.tx0, self.ty0, self.tx1, self.ty1 = tx0, ty0, tx1, ty1
+        self.removed, self.added, self.flipped = removed, added, flipped
+        self.dirty = np.asarray(dirty, np.int32)
+
+    def rect(self):
+        return (self.tx0, self.ty0, self.tx1, self.ty1)
+
+    def counts(self):
+        return (self.removed, self.added, self.flipped)
+
+
+class _CanvasBase:
+    def state(self) -> dict:
+        """Full canvas state in one layout: slots (n,2) f32, free (nfree,)
+        i32, inside/smask (tiles,) u64, spt (tiles*64,2) f32, sslot
+        (tiles*64,) i32, counts (slots, free, surface voxels, surface tiles)."""
+        raise NotImplementedError
+
+
+class Canvas(_CanvasBase):
+    """The oracle restatement (vo_canvas.c)."""
+
+    def __init__(self, width, height, voxel):
+        self.h = _canvas_lib().vo_canvas_create(width, height, voxel)
+        if not self.h:
+            raise MemoryError("vo_canvas_create")
+        self.dims = canvas_dims(width, height, voxel)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _canvas_lib().vo_canvas_destroy(self.h)
+            self.h = None
+
+    def rasterize(self, poly):
+        poly = np.ascontiguousarray(poly, np.float32).reshape(-1, 2)
+        if _canvas_lib().vo_canvas_rasterize(self.h, P(poly), len(poly)):
+            raise MemoryError("vo_canvas_rasterize")
+
+    def stamp(self, cx, cy, r, inside) -> CanvasEdit:
+        e = (C.c_int * 8)()
+        if _canvas_lib().vo_canvas_stamp(self.h, cx, cy, r, int(bool(inside)), C.byref(e)):
+            raise MemoryError("vo_canvas_stamp")
+        dirty = np.zeros(max(e[7], 1), np.int32)
+        _canvas_lib().vo_canvas_get(self.h, None, None, None, None, None, None, P(dirty))
+        return CanvasEdit(*e[:7], dirty=dirty[:e[7]])
+
+    def counts(self):
+        c = np.zeros(4, np.int64)
+        _canvas_lib().vo_canvas_counts(self.h, P(c))
+        return tuple(int(v) for v in c)
+
+    def slots(self) -> np.ndarray:
+        a = np.zeros((max(self.counts()[0], 1), 2), np.float32)
+        _canvas_lib().vo_canvas_get(self.h, P(a), None, None, None, None, None, None)
+        return a[:self.counts()[0]]
+
+    def inside(self) -> np.ndarray:
+        m = np.zeros(self.dims[2] * self.dims[3], np.uint64)
+        _canvas_lib().vo_canvas_get(self.h, None, None, P(m), None, None, None, None)
+        return m
+
+    def state(self) -> dict:
+        ns, nf, _, _ = self.counts()
+        tiles = self.dims[2] * self.dims[3]
+        st = dict(slots=np.zeros((max(ns, 1), 2), np.float32), free=np.zeros(max(nf, 1), np.int32),
+                  inside=np.zeros(tiles, np.uint64), smask=np.zeros(tiles, np.uint64),
+                  spt=np.zeros((tiles * 64, 2), np.float32), sslot=np.zeros(tiles * 64, np.int32))
+        _canvas_lib().vo_canvas_get(self.h, P(st["slots"]), P(st["free"]), P(st["inside"]), P(st["smask"]),
+                                    P(st["spt"]), P(st["sslot"]), None)
+        st["slots"], st["free"] = st["slots"][:ns], st["free"][:nf]
+        st["counts"] = self.counts()
+        return st
+
+
+class RefCanvas(_CanvasBase):
+    """The reference's own voromesh::Canvas, compiled from its sources."""
+
+    def __init__(self, width, height, voxel):
+        self.h = ref_canvas().rc_canvas_create(width, height, voxel)
+        self.dims = canvas_dims(width, height, voxel)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref_canvas().rc_canvas_destroy(self.h)
+            self.h = None
+
+    def rasterize(self, poly):
+        poly = np.ascontiguousarray(poly, np.float32).reshape(-1, 2)
+        ref_canvas().rc_canvas_rasterize(self.h, P(poly), len(poly))
+
+    def stamp(self, cx, cy, r, inside) -> CanvasEdit:
+        e = (C.c_int * 8)()
+        cap = 1 << 20
+        dirty = np.zeros(cap, np.int32)
+        ref_canvas().rc_canvas_stamp(self.h, cx, cy, r, int(bool(inside)), C.byref(e), P(dirty), cap)
+        return CanvasEdit(*e[:7], dirty=dirty[:e[7]].copy())
+
+    def counts(self):
+        c = np.zeros(4, np.int64)
+        ref_canvas().rc_canvas_counts(self.h, P(c))
+        return tuple(int(v) for v in c)
+
+    def state(self) -> dict:
+        ns, nf, _, _ = self.counts()
+        tiles = self.dims[2] * self.dims[3]
+        st = dict(slots=np.zeros((max(ns, 1), 2), np.float32), free=np.zeros(max(nf, 1), np.int32),
+                  inside=np.zeros(tiles, np.uint64), smask=np.zeros(tiles, np.uint64),
+                  spt=np.zeros((tiles * 64, 2), np.float32), sslot=np.zeros(tiles * 64, np.int32))
+        ref_canvas().rc_canvas_get(self.h, P(st["slots"]), P(st["free"]), P(st["inside"]), P(st["smask"]),
+                                   P(st["spt"]), P(st["sslot"]))
+        st["slots"], st["free"] = st["slots"][:ns], st["free"][:nf]
+        st["counts"] = self.counts()
+        return st
+
+
+def ref_make_heart(cx, cy, width, segments):
+    xy = np.zeros((segments, 2), np.float32)
+    ref_canvas().rc_make_heart(cx, cy, width, segments, P(xy))
+    return xy
+
+
+def canvas_relabelling(a: dict, b: dict):
+    """Checks that canvas states a and b are equal up to a relabelling of slot
+    indices and returns the map (a slot -> b slot). Occupancy, surface masks
+    and points, slot values, counts and free-list length must be identical;
+    slot indices must correspond one to one through the surface voxels and
+    the free-list positions. Raises AssertionError otherwise."""
+    assert a["counts"] == b["counts"], (a["counts"], b["counts"])
+    assert np.array_equal(a["inside"], b["inside"]), "occupancy differs"
+    assert np.array_equal(a["smask"], b["smask"]), "surface masks differ"
+    assert np.array_equal(a["spt"].view(np.uint32), b["spt"].view(np.uint32)), "surface points differ"
+    ns = a["counts"][0]
+    pi = np.full(ns, -1, np.int64)
+    on = a["sslot"] >= 0
+    assert np.array_equal(on, b["sslot"] >= 0)
+    src = np.concatenate([a["sslot"][on], a["free"]]).astype(np.int64)
+    dst = np.concatenate([b["sslot"][on], b["free"]]).astype(np.int64)
+    assert len(src) == ns, "slots are neither live nor free"
+    assert len(np.unique(src)) == ns and len(np.unique(dst)) == ns, "slot map is not one to one"
+    pi[src] = dst
+    assert np.array_equal(a["slots"].view(np.uint32), b["slots"][pi].view(np.uint32)), "slot values differ"
+    return pi

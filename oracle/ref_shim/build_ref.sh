@@ -9,6 +9,10 @@
 # by harness.cpp. -ffp-contract=off keeps a*b+c as two roundings, i.e. the
 # reference built with nvcc --fmad=false.
 #
+# It also compiles the reference's Canvas (src/voromesh/canvas.cpp and
+# shape2d.cpp, in place, with -I on its include/) and canvas_harness.cpp into
+# oracle/_ref/libref_canvas.so.
+#
 # Usage: REF=/path/to/reference bash oracle/ref_shim/build_ref.sh
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
@@ -37,3 +41,7 @@ section() { sed -n '/^namespace {$/,/^} \/\/ namespace$/p' "$1"; }
 } | ${CXX:-g++} -std=c++17 -O2 -fPIC -shared -ffp-contract=off -fno-fast-math -w -x c++ - \
     -o "$OUT/libref_kernels.so"
 echo "built $OUT/libref_kernels.so"
+${CXX:-g++} -std=c++20 -O2 -fPIC -shared -ffp-contract=off -fno-fast-math -w -I"$REF/include" \
+    "$REF/src/voromesh/canvas.cpp" "$REF/src/voromesh/shape2d.cpp" "$HERE/canvas_harness.cpp" \
+    -o "$OUT/libref_canvas.so"
+echo "built $OUT/libref_canvas.so"

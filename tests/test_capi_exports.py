@@ -21,7 +21,7 @@ def libpath():
 def _declared_c_functions():
     text = (ROOT / "include" / "vm_capi.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:vm|pd)_\w+)\s*\(", text, flags=re.M)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:vm|pd|cv)_\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
@@ -51,7 +51,11 @@ def test_cpp_classes_are_exported(libpath):
                 "voromesh::VoroOptimizer::Extract()", "voromesh::VoroOptimizer::BeginSchedule(int, int, int, int, int)",
                 "poisson::Sampler::Sampler(float, float, float, int, unsigned int)",
                 "poisson::Sampler::Resample(int, int, int, int)", "poisson::Sampler::Verify(int, int, int, int) const",
-                "voromesh::SetDefaultLossNeighbours(int)"]:
+                "voromesh::SetDefaultLossNeighbours(int)",
+                "voromesh::Canvas::Canvas(float, float, float)",
+                "voromesh::Canvas::StampDisc(voromesh::Vec2, float, bool)",
+                "voromesh::Canvas::RasterizeShape(std::vector<voromesh::Vec2, std::allocator<voromesh::Vec2> > const&)",
+                "voromesh::UpdateFromCanvas(voromesh::VoroOptimizer&, voromesh::Canvas const&)"]:
         assert sym in out, sym
 
 
@@ -62,5 +66,6 @@ def test_status_codes_without_gpu(libpath):
     lib = C.CDLL(str(libpath))
     assert lib.vm_create(C.c_float(-1.0), C.c_float(1.0), C.c_float(0.1), None, C.byref(C.c_void_p())) == 1
     assert lib.pd_create(C.c_float(1.0), C.c_float(1.0), C.c_float(0.0), 30, 1, C.byref(C.c_void_p())) == 1
+    assert lib.cv_create(C.c_float(1.0), C.c_float(1.0), C.c_float(0.0), C.byref(C.c_void_p())) == 1
     buf = C.create_string_buffer(256)
     assert lib.vm_last_error(buf, 256) == 0 and len(buf.value) > 0

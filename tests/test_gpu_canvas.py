@@ -1,0 +1,145 @@
+"""GPU canvas parity: RasterizeShape and StampDisc on the device equal the
+oracle's restatement of src/voromesh/canvas.cpp bit for bit (occupancy,
+surface masks and points, slot values and indices, free list, edit counts and
+dirty lists); the canvas-to-optimiser hand-off equals the host route."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(gpu_state, orc_state, orc):
+    pi = orc.canvas_relabelling(gpu_state, orc_state)
+    # the device visits rim voxels in the oracle's order: no relabelling at all
+    assert np.array_equal(pi, np.arange(len(pi)))
+    assert np.array_equal(gpu_state["free"], orc_state["free"])
+
+
+def _shapes():
+    from voromesh_gb300 import synth
+
+    yield "heart_1k", (1024.0, 1024.0, 1.0), synth.heart(512.0, 512.0, 819.2, 4096)
+    yield "heart_small_domain", (2.0, 2.0, 2.0 / 1024), synth.heart(1.0, 1.0, 1.6, 4096)
+    yield "odd_grid", (100.0, 61.0, 0.37), synth.heart(50.0, 30.0, 70.0, 50)
+    yield "triangle_outside", (64.0, 64.0, 1.0), np.array([[-10, -5], [80, 20], [20, 90]], np.float32)
+    # many vertices inside one voxel: dozens of samples per voxel
+    t = np.linspace(0, 2 * np.pi, 400, endpoint=False)
+    yield "tiny_ring", (16.0, 16.0, 1.0), np.stack([8.3 + 0.4 * np.cos(t), 8.6 + 0.4 * np.sin(t)], 1).astype(np.float32)
+    # 600 crossings on one scanline: the block-per-row path
+    yield "comb", (1000.0, 1000.0, 1.0), synth.comb(10.0, 10.0, 900.0, 500.0, 300)
+    # samples with coordinates of very different magnitude in one voxel: the
+    # sample-order fallback of the per-voxel sums
+    yield "tiny_coords", (8.0, 8.0, 1.0), np.array([[1e-30, 0.25], [0.75, 1e-25], [0.9, 0.9], [3.0, 7.0]], np.float32)
+    yield "single_vertex", (8.0, 8.0, 1.0), np.array([[3.5, 4.25]], np.float32)
+
+
+@pytest.mark.parametrize("name", [s[0] for s in _shapes()])
+def test_rasterize_bit_exact(vm, orc, name):
+    (w, h, vs), poly = next((d, p) for n, d, p in _shapes() if n == name)
+    c = vm.Canvas(w, h, vs)
+    c.RasterizeShape(poly)
+    o = orc.Canvas(w, h, vs)
+    o.rasterize(poly)
+    _same(c.state(), o.state(), orc)
+    c.close()
+
+
+def test_rasterize_empty_and_repeat(vm, orc):
+    from voromesh_gb300 import synth
+
+    c = vm.Canvas(64.0, 64.0, 1.0)
+    c.RasterizeShape(synth.heart(32.0, 32.0, 50.0, 300))
+    c.RasterizeShape(np.zeros((0, 2), np.float32))
+    assert c.SurfaceCount() == 0 and c.TargetSlots().shape == (0, 2) and not c.InsideMasks().any()
+    c.RasterizeShape(synth.heart(30.0, 33.0, 40.0, 200))
+    o = orc.Canvas(64.0, 64.0, 1.0)
+    o.rasterize(synth.heart(30.0, 33.0, 40.0, 200))
+    _same(c.state(), o.state(), orc)
+
+
+@pytest.mark.parametrize("w,vs,segs,seed", [(1024.0, 1.0, 4096, 1), (2.0, 2.0 / 1024, 4096, 2), (100.0, 0.37, 50, 3),
+                                            (64.0, 1.0, 7, 4)])
+def test_stamp_sequence_bit_exact(vm, orc, w, vs, segs, seed):
+    from voromesh_gb300 import synth
+
+    poly = synth.heart(0.5 * w, 0.5 * w, 0.8 * w, segs)
+    c = vm.Canvas(w, w, vs)
+    o = orc.Canvas(w, w, vs)
+    c.RasterizeShape(poly)
+    o.rasterize(poly)
+    rng = np.random.default_rng(seed)
+    for k in range(40):
+        cx, cy = rng.uniform(-0.1 * w, 1.1 * w, 2).astype(np.float32)
+        r = np.float32(rng.uniform(0.5, 0.15 * w / vs) * vs)
+        ins = bool(rng.integers(2))
+        eg = c.StampDisc((cx, cy), r, ins)
+        eo = o.stamp(cx, cy, r, ins)
+        assert (eg.tx0, eg.ty0, eg.tx1, eg.ty1) == eo.rect()
+        assert (eg.removed, eg.added, eg.flipped) == eo.counts()
+        assert np.array_equal(eg.dirtySlots, eo.dirty)
+        assert eg.Changed() == (sum(eo.counts()) > 0)
+        if k % 8 == 7:
+            _same(c.state(), o.state(), orc)
+    _same(c.state(), o.state(), orc)
+    assert c.SurfaceTileCount() == o.counts()[3]
+
+
+def test_stamp_edges(vm, orc):
+    """Stamps off the domain, of zero radius, covering the whole canvas, and
+    on a canvas never rasterised."""
+    from voromesh_gb300 import synth
+
+    c = vm.Canvas(64.0, 40.0, 1.0)
+    o = orc.Canvas(64.0, 40.0, 1.0)
+    seq = [(-100.0, -100.0, 5.0, True), (32.0, 20.0, 0.0, True), (10.0, 10.0, 6.0, True), (12.0, 12.0, 3.0, False),
+           (32.0, 20.0, 100.0, False), (32.0, 20.0, 8.0, True), (70.0, 45.0, 9.0, True), (0.0, 0.0, 2.5, False)]
+    for cx, cy, r, ins in seq:
+        eg = c.StampDisc((cx, cy), r, ins)
+        eo = o.stamp(cx, cy, r, ins)
+        assert (eg.tx0, eg.ty0, eg.tx1, eg.ty1) == eo.rect() and (eg.removed, eg.added, eg.flipped) == eo.counts()
+        assert np.array_equal(eg.dirtySlots, eo.dirty)
+    _same(c.state(), o.state(), orc)
+    poly = synth.heart(30.0, 20.0, 30.0, 64)
+    c.RasterizeShape(poly)
+    o.rasterize(poly)
+    _same(c.state(), o.state(), orc)
+
+
+def test_canvas_handoff_equals_host_route(vm):
+    """SetTargetsFromCanvas / UpdateFromCanvas (device to device) leave the
+    optimiser exactly as SetTargets/SetOccupancy and UpdateTargets/
+    UpdateOccupancy with the canvas's host arrays do (the editor's sequence,
+    apps/voromesh_demo.cpp:103-125)."""
+    from voromesh_gb300 import synth
+
+    W, vs, radius = 256.0, 1.0, 8.0
+    canvas = vm.Canvas(W, W, vs)
+    canvas.RasterizeShape(synth.heart(128.0, 128.0, 200.0, 1024))
+    sampler = vm.Sampler(W, W, radius, 30, 1)
+    params = vm.OptimizerParams(sampleFraction=0.2)
+    a = vm.VoroOptimizer(W, W, radius, params)
+    b = vm.VoroOptimizer(W, W, radius, params)
+    a.SetTargetsFromCanvas(canvas)
+    b.SetTargets(canvas.TargetSlots())
+    b.SetOccupancy(canvas.InsideMasks(), canvas.TilesX(), canvas.TilesY(), canvas.VoxelSize())
+    for o in (a, b):
+        o.SetGenerators(sampler.Cells(), sampler.GridW(), sampler.GridH(), sampler.CellSize())
+        o.BeginSchedule(60)
+        o.Optimize()
+    assert np.array_equal(a.Generators(), b.Generators())
+    rng = np.random.default_rng(5)
+    for k in range(6):
+        cx, cy = rng.uniform(60, 196, 2)
+        e = canvas.StampDisc((cx, cy), 14.0, bool(k % 2))
+        if not e.Changed():
+            continue
+        a.UpdateFromCanvas(canvas)
+        b.UpdateTargets(e.dirtySlots, canvas.TargetSlots())
+        b.UpdateOccupancy(canvas.InsideMasks(), e.tx0, e.ty0, e.tx1, e.ty1)
+        for o in (a, b):
+            o.BeginSchedule(20)
+            o.Optimize()
+        assert np.array_equal(a.Generators(), b.Generators())
+        assert a.EvaluateLoss() == b.EvaluateLoss()
+    ma, mb = a.Extract(), b.Extract()
+    assert np.array_equal(ma.inside, mb.inside) and np.array_equal(ma.vertices, mb.vertices)
