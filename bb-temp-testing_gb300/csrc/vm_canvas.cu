@@ -14,18 +14,20 @@
 //
 // Arithmetic follows the reference literally (IEEE float, no contraction;
 // the library is built with --fmad=false). Per-voxel means are double sums
-// of float samples; the reference adds them in sample order. Here they are
-// added in any order, with a certificate that makes that order-independent:
-// if every sample of a voxel is a multiple of the quantum Q of the smallest
-// one (always true for floats) and the sum of their magnitudes is below
-// 2^52 Q, every partial sum is an integer multiple of Q below 2^53 Q, hence
-// exact in double, in every order. Voxels without the certificate (samples of
-// wildly different magnitude) are summed again in sample order by one lane.
+// of float samples; the reference adds them in sample order. Every sample of
+// a voxel is an integer multiple of the quantum Q of its smallest one; when
+// their magnitudes sum to at most 2^52 Q, every partial sum in any order is
+// an integer multiple of Q below 2^53 Q, hence exact in double, so the
+// reference's sum is exactly the integer sum of the multiples times Q. That
+// integer sum is taken here (64-bit integers, no FP64 pipe in the loop).
+// Voxels without the certificate (samples of wildly different magnitude) are
+// summed again in double in sample order by one lane.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -44,6 +46,8 @@ constexpr int kRowCap = 512;      // crossings a warp sorts for one scanline
 constexpr int kBigCap = 32768;    // crossings one block sorts for one scanline
 constexpr int kMaxVoxelsX = 131072;
 constexpr int kBigBlocks = 32;
+constexpr int kListBlocks = 1024; // blocks of the tile work-list kernels (8 warps each)
+constexpr int kMaxBucketEntries = 1 << 27; // beyond this the scanline kernels test every edge
 
 enum { kErrSamples = 1, kErrCrossings = 2, kErrRimBox = 4 };
 
@@ -51,6 +55,8 @@ struct CvState {
     int nslots, nfree, surfaceTiles, err;
     long long surfaceCount;
     unsigned long long totalSamples;
+    int edgeEntries; // entries of the per-tile-row edge buckets
+    int listCount;   // tiles with samples (k_cv_tile_means work list)
     // last edit
     int removed, added, flipped, ndirty;
     int overflowRows;
@@ -103,16 +109,27 @@ __device__ int block_exclusive_scan(int v, int *sm, int &total)
     return ex;
 }
 
+constexpr int kPerThread = 8; // elements a thread scans serially per pass of a single-block scan
+
 __global__ void __launch_bounds__(1024) k_scan_single(const int *in, int *out, int n)
 {
     __shared__ int sm[32];
     int carry = 0;
-    for (int base = 0; base < n; base += 1024) {
-        int i = base + threadIdx.x;
-        int v = i < n ? in[i] : 0;
+    for (int base = 0; base < n; base += 1024 * kPerThread) {
+        int i0 = base + threadIdx.x * kPerThread;
+        int v[kPerThread], sum = 0;
+#pragma unroll
+        for (int k = 0; k < kPerThread; ++k) {
+            v[k] = i0 + k < n ? in[i0 + k] : 0;
+            sum += v[k];
+        }
         int tot;
-        int ex = block_exclusive_scan(v, sm, tot);
-        if (i < n) out[i] = carry + ex;
+        int run = carry + block_exclusive_scan(sum, sm, tot);
+#pragma unroll
+        for (int k = 0; k < kPerThread; ++k) {
+            if (i0 + k < n) out[i0 + k] = run;
+            run += v[k];
+        }
         carry += tot;
     }
     if (threadIdx.x == 0) out[n] = carry;
@@ -145,17 +162,34 @@ __global__ void __launch_bounds__(1024) k_scan3_single(int *a, int *b, int *c, i
 {
     __shared__ int sm[32];
     int ca = 0, cb = 0, cc = 0;
-    for (int base = 0; base < n; base += 1024) {
-        int i = base + threadIdx.x;
-        int va = i < n ? a[i] : 0, vb = i < n ? b[i] : 0, vc = i < n ? c[i] : 0;
+    constexpr int P = 8;
+    for (int base = 0; base < n; base += 1024 * P) {
+        int i0 = base + threadIdx.x * P;
+        int va[P], vb[P], vc[P], sa = 0, sb = 0, sc = 0;
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            bool in = i0 + k < n;
+            va[k] = in ? a[i0 + k] : 0;
+            vb[k] = in ? b[i0 + k] : 0;
+            vc[k] = in ? c[i0 + k] : 0;
+            sa += va[k];
+            sb += vb[k];
+            sc += vc[k];
+        }
         int ta, tb, tc;
-        int ea = block_exclusive_scan(va, sm, ta);
-        int eb = block_exclusive_scan(vb, sm, tb);
-        int ec = block_exclusive_scan(vc, sm, tc);
-        if (i < n) {
-            a[i] = ca + ea;
-            b[i] = cb + eb;
-            c[i] = cc + ec;
+        int ra = ca + block_exclusive_scan(sa, sm, ta);
+        int rb = cb + block_exclusive_scan(sb, sm, tb);
+        int rc = cc + block_exclusive_scan(sc, sm, tc);
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            if (i0 + k < n) {
+                a[i0 + k] = ra;
+                b[i0 + k] = rb;
+                c[i0 + k] = rc;
+            }
+            ra += va[k];
+            rb += vb[k];
+            rc += vc[k];
         }
         ca += ta;
         cb += tb;
@@ -184,38 +218,21 @@ __global__ void __launch_bounds__(1024) k_scan3_single(int *a, int *b, int *c, i
 // ---------------------------------------------------------------------------
 // per-voxel means of a tile's samples (shared by RasterizeShape and StampDisc)
 // ---------------------------------------------------------------------------
-struct WarpAcc {
-    double sx[64], sy[64], ax[64], ay[64];
-    int cnt[64], ex[64], ey[64];
-};
-
-__device__ __forceinline__ int quantum_exp(float v) // biased exponent of v's last bit position, >= 1
-{
-    int e = (int)((__float_as_uint(v) >> 23) & 0xFFu);
-    return e > 0 ? e : 1;
-}
-
-// Certificate: sum of magnitudes <= 2^52 * Q, Q = 2^(minExp - 150).
-__device__ __forceinline__ bool exact_any_order(double sumAbs, int minExp)
-{
-    if (minExp == INT_MAX) return true; // all samples zero
-    long long e = 1023 + 52 + (long long)minExp - 150;
-    return sumAbs <= __longlong_as_double(e << 52);
-}
-
-// The samples of voxel `bit` in sample order (canvas.cpp:13-25 adds them so).
-__device__ void ordered_sum(const float4 *rec, int beg, int end, int bit, int c, double &sx, double &sy)
+// The samples of one voxel's run (record indices run[0..n)) summed in
+// double in sample order (canvas.cpp:13-25 adds them so): repeated selection
+// of the next sample index.
+__device__ __noinline__ void ordered_sum(const float4 *rec, const int *run, int n, double &sx, double &sy)
 {
     sx = 0.0;
     sy = 0.0;
     int last = -1;
-    for (int k = 0; k < c; ++k) {
+    for (int k = 0; k < n; ++k) {
         int best = INT_MAX;
         float bx = 0.0f, by = 0.0f;
-        for (int r = beg; r < end; ++r) {
-            float4 q = rec[r];
+        for (int r = 0; r < n; ++r) {
+            float4 q = rec[run[r]];
             int id = __float_as_int(q.z);
-            if (__float_as_int(q.w) == bit && id > last && id < best) {
+            if (id > last && id < best) {
                 best = id;
                 bx = q.x;
                 by = q.y;
@@ -227,69 +244,182 @@ __device__ void ordered_sum(const float4 *rec, int beg, int end, int bit, int c,
     }
 }
 
-// One warp per tile with samples; rec = (x, y, sample index, bit) in tile
-// order (start[t] .. start[t+1]). Writes the tile's mask, the mean of each of
-// its voxels and the count of voxels; empty tiles get mask 0.
-__global__ void __launch_bounds__(256) k_cv_tile_means(const int *__restrict__ start, int nTiles,
-                                                        const float4 *__restrict__ rec,
+// Split of a float into sign, integer significand M and exponent e with
+// |v| = M * 2^(e - 150) (e = 1 for subnormals).
+__device__ __forceinline__ void float_split(float v, bool &neg, unsigned &M, int &e)
+{
+    unsigned u = __float_as_uint(v);
+    neg = (u >> 31) != 0;
+    int be = (int)((u >> 23) & 0xFFu);
+    M = u & 0x7FFFFFu;
+    if (be) M |= 0x800000u;
+    e = be > 0 ? be : 1;
+}
+
+// Exact mean of one voxel whose records are rec[perm[run[k]]], k < n.
+// Every sample is an integer multiple of Q = 2^(e0 - 150), where e0 is the
+// smallest exponent among the tile's non-zero samples (per axis). When the
+// voxel's magnitudes sum to at most 2^52 Q, every partial sum of its samples
+// in any order is an integer multiple of Q below 2^53 Q, hence exact in
+// double: the reference's sample-order double sum (canvas.cpp:13-25) equals
+// the 64-bit integer sum of the multiples times Q. Otherwise the samples are
+// summed in double in sample order.
+struct RunSums {
+    long long sx = 0, sy = 0;
+    unsigned long long ax = 0, ay = 0;
+    bool big = false;
+    __device__ void add(const float4 &q, int ex, int ey)
+    {
+        bool sg;
+        unsigned M;
+        int e;
+        float_split(q.x, sg, M, e);
+        if (M) {
+            int sh = e - ex;
+            big |= sh > 28;
+            unsigned long long t = sh > 28 ? 0ull : (unsigned long long)M << sh;
+            sx += sg ? -(long long)t : (long long)t;
+            ax += t;
+        }
+        float_split(q.y, sg, M, e);
+        if (M) {
+            int sh = e - ey;
+            big |= sh > 28;
+            unsigned long long t = sh > 28 ? 0ull : (unsigned long long)M << sh;
+            sy += sg ? -(long long)t : (long long)t;
+            ay += t;
+        }
+    }
+    __device__ float2 mean(const float4 *__restrict__ rec, const int *__restrict__ run, int n, int ex, int ey) const
+    {
+        const unsigned long long lim = 1ull << 52;
+        double x, y;
+        if (!big && ax <= lim && ay <= lim) {
+            x = ex == INT_MAX ? 0.0 : ldexp((double)sx, ex - 150);
+            y = ey == INT_MAX ? 0.0 : ldexp((double)sy, ey - 150);
+        } else {
+            ordered_sum(rec, run, n, x, y);
+        }
+        return make_float2((float)(x / (double)n), (float)(y / (double)n));
+    }
+};
+
+__device__ float2 voxel_mean(const float4 *__restrict__ rec, const int *__restrict__ run, int n, int ex, int ey)
+{
+    RunSums r;
+    for (int k = 0; k < n; ++k) r.add(rec[run[k]], ex, ey);
+    return r.mean(rec, run, n, ex, ey);
+}
+
+// The same for a long run, by the whole warp: lanes take every 32nd sample
+// and the integer sums are combined exactly by shuffles. Returns the mean on
+// every lane.
+__device__ float2 voxel_mean_warp(const float4 *__restrict__ rec, const int *__restrict__ run, int n, int ex, int ey)
+{
+    const int lane = threadIdx.x & 31;
+    RunSums r;
+    for (int k = lane; k < n; k += 32) r.add(rec[run[k]], ex, ey);
+    for (int o = 16; o > 0; o >>= 1) {
+        r.sx += __shfl_xor_sync(0xffffffffu, r.sx, o);
+        r.sy += __shfl_xor_sync(0xffffffffu, r.sy, o);
+        r.ax += __shfl_xor_sync(0xffffffffu, r.ax, o);
+        r.ay += __shfl_xor_sync(0xffffffffu, r.ay, o);
+    }
+    r.big = __any_sync(0xffffffffu, r.big);
+    float2 m = make_float2(0.0f, 0.0f);
+    if (lane == 0) m = r.mean(rec, run, n, ex, ey);
+    m.x = __shfl_sync(0xffffffffu, m.x, 0);
+    m.y = __shfl_sync(0xffffffffu, m.y, 0);
+    return m;
+}
+
+constexpr int kLaneRun = 32; // longer voxel runs are reduced by the whole warp
+
+// Counting sort of one tile's records by voxel (one set per warp).
+struct TileSort {
+    int cnt[64], off[64], fill[64];
+};
+
+// One warp per tile of the work list (the tiles that received samples, in
+// any order); rec = (x, y, sample index, bit) in tile order (start[t] ..
+// start[t+1]). The warp sorts the tile's records by voxel (perm, a scratch
+// array as long as rec), then lane l reduces the runs of voxels l and l + 32
+// (runs longer than kLaneRun: the whole warp).
+// Writes the tile's mask, the mean of each of its voxels and the count of
+// voxels. Tiles off the list keep the zero masks and counts they were
+// cleared to.
+__global__ void __launch_bounds__(256, 2) k_cv_tile_means(const int *__restrict__ list, const int *listCount,
+                                                        const int *__restrict__ start, const float4 *__restrict__ rec,
+                                                        int *__restrict__ perm,
                                                         unsigned long long *__restrict__ outMask,
                                                         float2 *__restrict__ outPt, int *__restrict__ outCount,
                                                         int *surfaceTiles)
 {
-    __shared__ WarpAcc acc[8];
+    __shared__ TileSort sorts[8];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    WarpAcc &A = acc[wib];
-    const int warps = gridDim.x * 8;
-    for (int base = (blockIdx.x * 8 + wib) * 32; base < nTiles; base += warps * 32) {
-        int t = base + lane;
-        int c = t < nTiles ? start[t + 1] - start[t] : 0;
-        if (t < nTiles && c == 0) {
-            outMask[t] = 0ull;
-            if (outCount) outCount[t] = 0;
+    TileSort &T = sorts[wib];
+    const int nList = *listCount;
+    for (int k = blockIdx.x * 8 + wib; k < nList; k += gridDim.x * 8) {
+        const int tile = list[k];
+        const int beg = start[tile], end = start[tile + 1];
+        T.cnt[lane] = T.cnt[lane + 32] = 0;
+        T.fill[lane] = T.fill[lane + 32] = 0;
+        __syncwarp();
+        int ex = INT_MAX, ey = INT_MAX;
+        for (int r = beg + lane; r < end; r += 32) {
+            const float4 q = rec[r];
+            atomicAdd(&T.cnt[__float_as_int(q.w)], 1);
+            bool sg;
+            unsigned M;
+            int e;
+            float_split(q.x, sg, M, e);
+            if (M) ex = min(ex, e);
+            float_split(q.y, sg, M, e);
+            if (M) ey = min(ey, e);
         }
-        unsigned todo = __ballot_sync(0xffffffffu, c > 0);
-        while (todo) {
-            int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            int tile = base + src;
-            int beg = start[tile], end = start[tile + 1];
-            for (int b = lane; b < 64; b += 32) {
-                A.sx[b] = A.sy[b] = A.ax[b] = A.ay[b] = 0.0;
-                A.cnt[b] = 0;
-                A.ex[b] = A.ey[b] = INT_MAX;
+        ex = __reduce_min_sync(0xffffffffu, ex);
+        ey = __reduce_min_sync(0xffffffffu, ey);
+        __syncwarp();
+        // exclusive offsets of the 64 voxel runs
+        const int c0 = T.cnt[lane], c1 = T.cnt[lane + 32];
+        int i0 = c0, i1 = c1;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y0 = __shfl_up_sync(0xffffffffu, i0, o), y1 = __shfl_up_sync(0xffffffffu, i1, o);
+            if (lane >= o) {
+                i0 += y0;
+                i1 += y1;
             }
-            __syncwarp();
-            for (int r = beg + lane; r < end; r += 32) {
-                float4 q = rec[r];
-                int b = __float_as_int(q.w);
-                atomicAdd(&A.sx[b], (double)q.x);
-                atomicAdd(&A.sy[b], (double)q.y);
-                atomicAdd(&A.ax[b], fabs((double)q.x));
-                atomicAdd(&A.ay[b], fabs((double)q.y));
-                atomicAdd(&A.cnt[b], 1);
-                if (q.x != 0.0f) atomicMin(&A.ex[b], quantum_exp(q.x));
-                if (q.y != 0.0f) atomicMin(&A.ey[b], quantum_exp(q.y));
-            }
-            __syncwarp();
-            unsigned long long mask = 0ull;
-            for (int half = 0; half < 2; ++half) {
-                int b = lane + 32 * half;
-                int n = A.cnt[b];
-                if (n > 0) {
-                    double sx = A.sx[b], sy = A.sy[b];
-                    if (!exact_any_order(A.ax[b], A.ex[b]) || !exact_any_order(A.ay[b], A.ey[b]))
-                        ordered_sum(rec, beg, end, b, n, sx, sy);
-                    outPt[(size_t)tile * 64 + b] = make_float2((float)(sx / (double)n), (float)(sy / (double)n));
-                }
-                mask |= (unsigned long long)__ballot_sync(0xffffffffu, n > 0) << (32 * half);
-            }
-            if (lane == 0) {
-                outMask[tile] = mask;
-                if (outCount) outCount[tile] = __popcll(mask);
-                if (surfaceTiles && mask) atomicAdd(surfaceTiles, 1);
-            }
-            __syncwarp();
         }
+        const int tot0 = __shfl_sync(0xffffffffu, i0, 31);
+        T.off[lane] = i0 - c0;
+        T.off[lane + 32] = tot0 + i1 - c1;
+        __syncwarp();
+        for (int r = beg + lane; r < end; r += 32) {
+            const int b = __float_as_int(rec[r].w);
+            perm[beg + T.off[b] + atomicAdd(&T.fill[b], 1)] = r;
+        }
+        __syncwarp();
+        // runs of up to kLaneRun samples: one lane each; longer runs: the whole warp
+        if (c0 > 0 && c0 <= kLaneRun)
+            outPt[(size_t)tile * 64 + lane] = voxel_mean(rec, perm + beg + T.off[lane], c0, ex, ey);
+        if (c1 > 0 && c1 <= kLaneRun)
+            outPt[(size_t)tile * 64 + lane + 32] = voxel_mean(rec, perm + beg + T.off[lane + 32], c1, ex, ey);
+        unsigned long long longRuns = (unsigned long long)__ballot_sync(0xffffffffu, c0 > kLaneRun) |
+                                      ((unsigned long long)__ballot_sync(0xffffffffu, c1 > kLaneRun) << 32);
+        while (longRuns) {
+            const int b = __ffsll((long long)longRuns) - 1;
+            longRuns &= longRuns - 1;
+            const float2 m = voxel_mean_warp(rec, perm + beg + T.off[b], T.cnt[b], ex, ey);
+            if (lane == 0) outPt[(size_t)tile * 64 + b] = m;
+        }
+        const unsigned long long mask = (unsigned long long)__ballot_sync(0xffffffffu, c0 > 0) |
+                                        ((unsigned long long)__ballot_sync(0xffffffffu, c1 > 0) << 32);
+        if (lane == 0) {
+            outMask[tile] = mask;
+            if (outCount) outCount[tile] = __popcll(mask);
+            if (surfaceTiles && mask) atomicAdd(surfaceTiles, 1);
+        }
+        __syncwarp();
     }
 }
 
@@ -300,22 +430,26 @@ __global__ void k_cv_seg_counts(const float2 *__restrict__ poly, int n, float st
                                 CvState *st)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    float2 a = poly[s], b = poly[s + 1 == n ? 0 : s + 1];
-    float dx = b.x - a.x, dy = b.y - a.y;
-    // hypot: both squares are exact in double, so this is the correctly
-    // rounded root of the exact sum, rounded once more to float
-    float len = (float)sqrt((double)dx * (double)dx + (double)dy * (double)dy);
-    float q = ceilf(len / step);
-    int m;
-    if (q < 16777216.0f) {
-        m = q > 1.0f ? (int)q : 1;
-    } else {
-        m = 1;
-        atomicOr(&st->err, kErrSamples);
+    int m = 0;
+    if (s < n) {
+        float2 a = poly[s], b = poly[s + 1 == n ? 0 : s + 1];
+        float dx = b.x - a.x, dy = b.y - a.y;
+        // hypot: both squares are exact in double, so this is the correctly
+        // rounded root of the exact sum, rounded once more to float
+        float len = (float)sqrt((double)dx * (double)dx + (double)dy * (double)dy);
+        float q = ceilf(len / step);
+        if (q < 16777216.0f) {
+            m = q > 1.0f ? (int)q : 1;
+        } else {
+            m = 1;
+            atomicOr(&st->err, kErrSamples);
+        }
+        cnt[s] = m;
     }
-    cnt[s] = m;
-    atomicAdd(&st->totalSamples, (unsigned long long)m);
+    // the 64-bit total (the int scan must not overflow): one atomic per warp
+    unsigned long long w = (unsigned long long)m;
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&st->totalSamples, w);
 }
 
 __device__ __forceinline__ bool voxel_of(float x, float y, const CvGeom &g, int &i, int &j)
@@ -330,30 +464,43 @@ __device__ __forceinline__ bool voxel_of(float x, float y, const CvGeom &g, int 
 
 __global__ void k_cv_samples(const float2 *__restrict__ poly, int n, const int *__restrict__ segStart, int total,
                              CvGeom g, int *__restrict__ tileCount, int *__restrict__ recTile,
-                             int *__restrict__ recRank, float2 *__restrict__ recXY)
+                             int *__restrict__ recRank, float2 *__restrict__ recXY, int *__restrict__ list,
+                             CvState *st)
 {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int tile = -1;
+    float x = 0.0f, y = 0.0f;
+    if (idx < total) {
+        // segment s: the last with segStart[s] <= idx
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (segStart[mid] <= idx) lo = mid;
+            else hi = mid - 1;
+        }
+        int s = lo;
+        int m = segStart[s + 1] - segStart[s], k = idx - segStart[s];
+        float2 a = poly[s], b = poly[s + 1 == n ? 0 : s + 1];
+        float t = (float)k / (float)m;
+        x = a.x + t * (b.x - a.x);
+        y = a.y + t * (b.y - a.y);
+        int i, j;
+        if (voxel_of(x, y, g, i, j)) tile = (j >> 3) * g.tilesX + (i >> 3);
+    }
+    // consecutive samples mostly share a tile: one atomic per tile and warp
+    const unsigned grp = __match_any_sync(0xffffffffu, tile);
+    const int leader = __ffs(grp) - 1;
+    int base = 0;
+    if (lane == leader && tile >= 0) {
+        base = atomicAdd(&tileCount[tile], __popc(grp));
+        if (base == 0) list[atomicAdd(&st->listCount, 1)] = tile;
+    }
+    base = __shfl_sync(0xffffffffu, base, leader);
     if (idx >= total) return;
-    // segment s: the last with segStart[s] <= idx
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (segStart[mid] <= idx) lo = mid;
-        else hi = mid - 1;
-    }
-    int s = lo;
-    int m = segStart[s + 1] - segStart[s], k = idx - segStart[s];
-    float2 a = poly[s], b = poly[s + 1 == n ? 0 : s + 1];
-    float t = (float)k / (float)m;
-    float x = a.x + t * (b.x - a.x), y = a.y + t * (b.y - a.y);
-    int i, j;
-    if (!voxel_of(x, y, g, i, j)) {
-        recTile[idx] = -1;
-        return;
-    }
-    int tile = (j >> 3) * g.tilesX + (i >> 3);
     recTile[idx] = tile;
-    recRank[idx] = atomicAdd(&tileCount[tile], 1);
+    if (tile < 0) return;
+    recRank[idx] = base + __popc(grp & ((1u << lane) - 1u));
     recXY[idx] = make_float2(x, y);
 }
 
@@ -371,36 +518,30 @@ __global__ void k_cv_scatter(int total, const int *__restrict__ recTile, const i
 }
 
 // Slots in tile-major voxel order (canvas.cpp:96-114): slot = surface voxels
-// before this one.
-__global__ void __launch_bounds__(256) k_cv_assign(const unsigned long long *__restrict__ smask,
+// before this one. One warp per tile of the work list.
+__global__ void __launch_bounds__(256) k_cv_assign(const int *__restrict__ list, const int *listCount,
+                                                    const unsigned long long *__restrict__ smask,
                                                     const int *__restrict__ surfStart, int nTiles,
                                                     const float2 *__restrict__ spt, int *__restrict__ sslot,
                                                     float2 *__restrict__ slots, CvState *st)
 {
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int warps = gridDim.x * 8;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         st->nslots = surfStart[nTiles];
         st->nfree = 0;
         st->surfaceCount = surfStart[nTiles];
     }
-    for (int base = (blockIdx.x * 8 + wib) * 32; base < nTiles; base += warps * 32) {
-        int t = base + lane;
-        unsigned long long m = t < nTiles ? smask[t] : 0ull;
-        unsigned todo = __ballot_sync(0xffffffffu, m != 0ull);
-        while (todo) {
-            int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            int tile = base + src;
-            unsigned long long mask = __shfl_sync(0xffffffffu, m, src);
-            int s0 = surfStart[tile];
-            for (int b = lane; b < 64; b += 32) {
-                if (!((mask >> b) & 1ull)) continue;
-                int slot = s0 + __popcll(mask & lower_bits(b));
-                size_t v = (size_t)tile * 64 + b;
-                sslot[v] = slot;
-                slots[slot] = spt[v];
-            }
+    const int nList = *listCount;
+    for (int k = blockIdx.x * 8 + wib; k < nList; k += gridDim.x * 8) {
+        const int tile = list[k];
+        const unsigned long long mask = smask[tile];
+        const int s0 = surfStart[tile];
+        for (int b = lane; b < 64; b += 32) {
+            if (!((mask >> b) & 1ull)) continue;
+            int slot = s0 + __popcll(mask & lower_bits(b));
+            size_t v = (size_t)tile * 64 + b;
+            sslot[v] = slot;
+            slots[slot] = spt[v];
         }
     }
 }
@@ -432,18 +573,96 @@ __device__ __forceinline__ float crossing(float2 a, float2 b, float y)
     return a.x + (y - a.y) * (b.x - a.x) / (b.y - a.y);
 }
 
+// Tile rows whose scanlines edge (a, b) can cross: rows j with centre
+// (j + 0.5) * vs between the edge's end ordinates, widened by one row each
+// way for rounding. Horizontal edges cross none.
+__device__ __forceinline__ bool edge_tile_rows(float2 a, float2 b, const CvGeom &g, int &r0, int &r1)
+{
+    if (a.y == b.y) return false;
+    float lo = fminf(a.y, b.y), hi = fmaxf(a.y, b.y);
+    float jlo = fmaxf(floorf(lo * g.inv - 0.5f) - 1.0f, 0.0f);
+    float jhi = fminf(ceilf(hi * g.inv - 0.5f) + 1.0f, (float)(g.vy - 1));
+    if (!(jlo <= jhi)) return false;
+    r0 = (int)jlo >> 3;
+    r1 = (int)jhi >> 3;
+    return true;
+}
+
+// Edge buckets per tile row: count, then (after a scan) fill. An edge is
+// (s, s - 1), the reference's pairing (canvas.cpp:121).
+// Edges within one tile row (most of them) are grouped per warp: one atomic
+// per row and warp; edges spanning several rows count row by row.
+__device__ __forceinline__ int edge_key(const float2 *__restrict__ poly, int n, const CvGeom &g, int s, int &r0,
+                                        int &r1)
+{
+    const int lane = threadIdx.x & 31;
+    if (s >= n || !edge_tile_rows(poly[s], poly[s == 0 ? n - 1 : s - 1], g, r0, r1)) {
+        r0 = 0;
+        r1 = -1;
+        return -1 - lane;
+    }
+    return r0 == r1 ? r0 : -1 - lane;
+}
+
+__global__ void k_cv_edge_count(const float2 *__restrict__ poly, int n, CvGeom g, int *__restrict__ rowCount)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int r0, r1;
+    const int key = edge_key(poly, n, g, s, r0, r1);
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    if (key >= 0) {
+        if (lane == __ffs(grp) - 1) atomicAdd(&rowCount[key], __popc(grp));
+    } else {
+        for (int r = r0; r <= r1; ++r) atomicAdd(&rowCount[r], 1);
+    }
+}
+
+__global__ void k_cv_edge_fill(const float2 *__restrict__ poly, int n, CvGeom g, const int *__restrict__ rowStart,
+                               int *__restrict__ rowFill, int *__restrict__ bucket)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int r0, r1;
+    const int key = edge_key(poly, n, g, s, r0, r1);
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(grp) - 1;
+    int base = 0;
+    if (key >= 0 && lane == leader) base = atomicAdd(&rowFill[key], __popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key >= 0) {
+        bucket[rowStart[key] + base + __popc(grp & ((1u << lane) - 1u))] = s;
+    } else {
+        for (int r = r0; r <= r1; ++r) bucket[rowStart[r] + atomicAdd(&rowFill[r], 1)] = s;
+    }
+}
+
+// The edges of tile row ty staged in shared memory as (a.x, a.y, b.x, b.y):
+// the row's bucket, or every edge when there are no buckets.
+__device__ __forceinline__ void stage_edges(const float2 *__restrict__ poly, int n, const int *__restrict__ bucket,
+                                            int c0, int m, float4 *ch)
+{
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        int e = bucket ? bucket[c0 + k] : c0 + k;
+        float2 a = poly[e], b = poly[e == 0 ? n - 1 : e - 1];
+        ch[k] = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
 // One block per tile row, one warp per scanline. Crossings are gathered in
 // shared memory, sorted (bitonic) and turned into spans of a row bitmap; the
 // block then writes whole tile words. Rows with more than kRowCap crossings
-// are left for k_cv_scanline_big.
-__global__ void __launch_bounds__(256) k_cv_scanline(const float2 *__restrict__ poly, int n, CvGeom g,
-                                                      unsigned long long *__restrict__ inside, int *ovRows,
+// are left for k_cv_scanline_big. With buckets (rowStart/bucket non-null) a
+// block tests only the edges that can reach its rows; otherwise all of them.
+__global__ void __launch_bounds__(256) k_cv_scanline(const float2 *__restrict__ poly, int n,
+                                                      const int *__restrict__ rowStart, const int *__restrict__ bucket,
+                                                      CvGeom g, unsigned long long *__restrict__ inside, int *ovRows,
                                                       CvState *st)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int W32 = (g.vx + 31) >> 5;
-    float2 *ch = reinterpret_cast<float2 *>(smraw);
-    float *buf = reinterpret_cast<float *>(ch + kChunk + 1);
+    float4 *ch = reinterpret_cast<float4 *>(smraw);
+    float *buf = reinterpret_cast<float *>(ch + kChunk);
     int *cnt = reinterpret_cast<int *>(buf + 8 * kRowCap);
     unsigned *bits = reinterpret_cast<unsigned *>(cnt + 8);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -453,18 +672,16 @@ __global__ void __launch_bounds__(256) k_cv_scanline(const float2 *__restrict__ 
     const float y = ((float)j + 0.5f) * g.vs;
     for (int k = threadIdx.x; k < 8 * W32; k += 256) bits[k] = 0u;
     if (lane == 0) cnt[w] = 0;
-    for (int c0 = 0; c0 < n; c0 += kChunk) {
-        int m = min(kChunk, n - c0);
+    const int e0 = bucket ? rowStart[ty] : 0, e1 = bucket ? rowStart[ty + 1] : n;
+    for (int c0 = e0; c0 < e1; c0 += kChunk) {
+        int m = min(kChunk, e1 - c0);
         __syncthreads();
-        // ch[k] = poly[c0 + k - 1] (poly[n - 1] before vertex 0)
-        for (int k = threadIdx.x; k <= m; k += 256) {
-            int s = c0 + k - 1;
-            ch[k] = poly[s < 0 ? n - 1 : s];
-        }
+        stage_edges(poly, n, bucket, c0, m, ch);
         __syncthreads();
         if (live) {
             for (int k = lane; k < m; k += 32) {
-                float2 a = ch[k + 1], b = ch[k]; // edge (s, s - 1)
+                float4 q = ch[k];
+                float2 a = make_float2(q.x, q.y), b = make_float2(q.z, q.w); // edge (s, s - 1)
                 if ((a.y > y) != (b.y > y)) {
                     float x = crossing(a, b, y);
                     int p = atomicAdd(&cnt[w], 1);
@@ -515,7 +732,9 @@ __global__ void __launch_bounds__(256) k_cv_scanline(const float2 *__restrict__ 
 // Rows with more than kRowCap crossings: one block per row, up to kBigCap
 // crossings sorted in shared memory; the row's byte of each tile word is
 // written directly (the rows of one tile row own distinct bytes).
-__global__ void __launch_bounds__(1024) k_cv_scanline_big(const float2 *__restrict__ poly, int n, CvGeom g,
+__global__ void __launch_bounds__(1024) k_cv_scanline_big(const float2 *__restrict__ poly, int n,
+                                                           const int *__restrict__ rowStart,
+                                                           const int *__restrict__ bucket, CvGeom g,
                                                            unsigned long long *__restrict__ inside,
                                                            const int *__restrict__ ovRows, CvState *st)
 {
@@ -531,7 +750,9 @@ __global__ void __launch_bounds__(1024) k_cv_scanline_big(const float2 *__restri
         if (threadIdx.x == 0) cnt = 0;
         for (int k = threadIdx.x; k < W32; k += blockDim.x) row[k] = 0u;
         __syncthreads();
-        for (int s = threadIdx.x; s < n; s += blockDim.x) {
+        const int e0 = bucket ? rowStart[j >> 3] : 0, e1 = bucket ? rowStart[(j >> 3) + 1] : n;
+        for (int k = e0 + threadIdx.x; k < e1; k += blockDim.x) {
+            int s = bucket ? bucket[k] : k;
             float2 a = poly[s], b = poly[s == 0 ? n - 1 : s - 1];
             if ((a.y > y) != (b.y > y)) {
                 float x = crossing(a, b, y);
@@ -583,7 +804,8 @@ __global__ void __launch_bounds__(1024) k_cv_scanline_big(const float2 *__restri
 //    of the stamp's tile box (canvas.cpp:148-158)
 __global__ void k_cv_rim_bin(const float2 *__restrict__ rimXY, CvStamp p, CvGeom g,
                              const unsigned long long *__restrict__ inside, int *__restrict__ boxCount,
-                             int *__restrict__ recTile, int *__restrict__ recRank, CvState *st)
+                             int *__restrict__ recTile, int *__restrict__ recRank, int *__restrict__ list,
+                             CvState *st)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= p.nRim) return;
@@ -600,7 +822,9 @@ __global__ void k_cv_rim_bin(const float2 *__restrict__ rimXY, CvStamp p, CvGeom
     }
     int lt = ty * p.bw + tx;
     recTile[k] = lt;
-    recRank[k] = atomicAdd(&boxCount[lt], 1);
+    int rank = atomicAdd(&boxCount[lt], 1);
+    recRank[k] = rank;
+    if (rank == 0) list[atomicAdd(&st->listCount, 1)] = lt;
 }
 
 // 2-3. per box tile: surface samples strictly inside the disc (removed),
@@ -755,7 +979,7 @@ __global__ void k_cv_copy_rect(const unsigned long long *__restrict__ src, unsig
 
 cudaError_t scan_ex(const int *in, int *out, int n, int *partial, cudaStream_t s)
 {
-    if (n <= 16384) {
+    if (n <= 8192) {
         k_scan_single<<<1, 1024, 0, s>>>(in, out, n);
     } else {
         int nb = (n + kScanChunk - 1) / kScanChunk;
@@ -766,7 +990,7 @@ cudaError_t scan_ex(const int *in, int *out, int n, int *partial, cudaStream_t s
     return cudaGetLastError();
 }
 
-int scan_partials(int n) { return n <= 16384 ? 1 : (n + kScanChunk - 1) / kScanChunk + 1; }
+int scan_partials(int n) { return n <= 8192 ? 1 : (n + kScanChunk - 1) / kScanChunk + 1; }
 
 } // namespace
 
@@ -787,6 +1011,8 @@ struct cv_canvas {
     DevBuf<unsigned long long> inside, smask;
     DevBuf<float2> spt, slots, recXY, poly, rimPt, dirtyVal;
     DevBuf<int> sslot, freel, dirty, segCnt, tileCount, surfCount, partial, recTile, recRank, ovRows;
+    DevBuf<int> rowStart, rowFill, bucket; // edge buckets per tile row
+    DevBuf<int> tileList;                  // tiles with samples
     DevBuf<float4> rec;
     DevBuf<CvState> dState;
     // stamp scratch
@@ -867,7 +1093,7 @@ int cv_create(float width, float height, float voxelSize, cv_canvas **out)
         return rc;
     }
     int W32 = (c->g.vx + 31) / 32;
-    c->smemScan = (int)((kChunk + 1) * sizeof(float2) + 8 * kRowCap * sizeof(float) + 8 * sizeof(int) +
+    c->smemScan = (int)(kChunk * sizeof(float4) + 8 * kRowCap * sizeof(float) + 8 * sizeof(int) +
                         8 * (size_t)W32 * sizeof(unsigned));
     c->smemBig = (int)(kBigCap * sizeof(float) + (size_t)W32 * sizeof(unsigned));
     if ((e = cudaFuncSetAttribute(k_cv_scanline, cudaFuncAttributeMaxDynamicSharedMemorySize, c->smemScan)) ||
@@ -898,6 +1124,8 @@ int cv_destroy(cv_canvas *c)
 int cv_rasterize(cv_canvas *c, const float *xy, int n, float *gpuMs)
 {
     if (!c || n < 0 || (n > 0 && !xy)) return fail(VM_ERR_ARG, "cv_rasterize: bad arguments");
+    for (long long k = 0; k < 2LL * n; ++k)
+        if (!std::isfinite(xy[k])) return fail(VM_ERR_ARG, "cv_rasterize: polygon coordinates must be finite");
     cudaStream_t s = c->stream;
     const CvGeom g = c->g;
     const int T = (int)c->tiles;
@@ -909,38 +1137,68 @@ int cv_rasterize(cv_canvas *c, const float *xy, int n, float *gpuMs)
         return cuda_fail(e, "cv_rasterize");
     if (n > 0) {
         if ((rc = c->poly.reserve(n)) || (rc = c->segCnt.reserve((size_t)n + 1)) ||
-            (rc = c->partial.reserve((size_t)std::max(scan_partials(n + 1), scan_partials(T + 1)))))
+            (rc = c->partial.reserve((size_t)std::max(scan_partials(n + 1), scan_partials(T + 1)))) ||
+            (rc = c->rowStart.reserve((size_t)g.tilesY + 1)) || (rc = c->rowFill.reserve((size_t)g.tilesY + 1)))
             return rc;
-        if ((e = cudaMemcpyAsync(c->poly.p, xy, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, s)))
+        if ((e = cudaMemcpyAsync(c->poly.p, xy, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemsetAsync(c->rowStart.p, 0, sizeof(int) * ((size_t)g.tilesY + 1), s)))
             return cuda_fail(e, "upload polygon");
         k_cv_seg_counts<<<blocks_for(n, 256), 256, 0, s>>>(c->poly.p, n, 0.25f * g.vs, c->segCnt.p, c->dState.p);
         if ((e = scan_ex(c->segCnt.p, c->segCnt.p, n, c->partial.p, s))) return cuda_fail(e, "segment scan");
+        // edge buckets per tile row (sized by the same read-back as the samples)
+        k_cv_edge_count<<<blocks_for(n, 256), 256, 0, s>>>(c->poly.p, n, g, c->rowStart.p);
+        if ((e = scan_ex(c->rowStart.p, c->rowStart.p, g.tilesY, c->partial.p, s)) ||
+            (e = cudaMemcpyAsync(&c->dState.p->edgeEntries, c->rowStart.p + g.tilesY, sizeof(int),
+                                 cudaMemcpyDeviceToDevice, s)))
+            return cuda_fail(e, "edge buckets");
         if ((rc = read_state(c))) return rc;
         if (c->st.err & kErrSamples) return fail(VM_ERR_UNSUPPORTED, "cv_rasterize: a polygon edge spans too many voxels");
         if (c->st.totalSamples > (unsigned long long)INT_MAX) return fail(VM_ERR_UNSUPPORTED, "cv_rasterize: too many surface samples");
         const int total = (int)c->st.totalSamples;
         if ((rc = c->recTile.reserve(total)) || (rc = c->recRank.reserve(total)) || (rc = c->recXY.reserve(total)) ||
             (rc = c->rec.reserve(total)) || (rc = c->tileCount.reserve((size_t)T + 1)) ||
-            (rc = c->surfCount.reserve((size_t)T + 1)))
+            (rc = c->surfCount.reserve((size_t)T + 1)) || (rc = c->tileList.reserve((size_t)std::min(T, total))))
             return rc;
         // a surface voxel holds at least one sample: `total` bounds the slots
         size_t cap = (size_t)std::min<long long>(total, (long long)T * 64);
         if ((rc = c->slots.reserve(std::max<size_t>(cap, 1))) || (rc = c->freel.reserve(std::max<size_t>(cap, 1))))
             return rc;
-        if ((e = cudaMemsetAsync(c->tileCount.p, 0, sizeof(int) * ((size_t)T + 1), s))) return cuda_fail(e, "memset");
+        if ((e = cudaMemsetAsync(c->tileCount.p, 0, sizeof(int) * ((size_t)T + 1), s)) ||
+            (e = cudaMemsetAsync(c->surfCount.p, 0, sizeof(int) * ((size_t)T + 1), s)))
+            return cuda_fail(e, "memset");
+        // VM_CANVAS_BUCKET_CAP lowers the bucket limit (0 = always test every edge)
+        long long bucketCap = kMaxBucketEntries;
+        if (const char *env = std::getenv("VM_CANVAS_BUCKET_CAP")) bucketCap = std::min(bucketCap, std::atoll(env));
+        const int entries = c->st.edgeEntries;
+        const bool buckets = entries >= 0 && entries <= bucketCap && bucketCap > 0;
+        if (buckets) {
+            if ((rc = c->bucket.reserve((size_t)std::max(entries, 1)))) return rc;
+            if ((e = cudaMemsetAsync(c->rowFill.p, 0, sizeof(int) * ((size_t)g.tilesY + 1), s)))
+                return cuda_fail(e, "memset");
+            k_cv_edge_fill<<<blocks_for(n, 256), 256, 0, s>>>(c->poly.p, n, g, c->rowStart.p, c->rowFill.p,
+                                                              c->bucket.p);
+        }
+        const int *rs = buckets ? c->rowStart.p : nullptr;
+        const int *bk = buckets ? c->bucket.p : nullptr;
         k_cv_samples<<<blocks_for(total, 256), 256, 0, s>>>(c->poly.p, n, c->segCnt.p, total, g, c->tileCount.p,
-                                                            c->recTile.p, c->recRank.p, c->recXY.p);
+                                                            c->recTile.p, c->recRank.p, c->recXY.p, c->tileList.p,
+                                                            c->dState.p);
         if ((e = scan_ex(c->tileCount.p, c->tileCount.p, T, c->partial.p, s))) return cuda_fail(e, "tile scan");
         k_cv_scatter<<<blocks_for(total, 256), 256, 0, s>>>(total, c->recTile.p, c->recRank.p, c->recXY.p,
                                                             c->tileCount.p, g, c->rec.p);
-        int warpBlocks = blocks_for(T, 256);
-        k_cv_tile_means<<<warpBlocks, 256, 0, s>>>(c->tileCount.p, T, c->rec.p, c->smask.p, c->spt.p, c->surfCount.p,
-                                                   &c->dState.p->surfaceTiles);
+        const int listGrid = std::min(blocks_for(std::min(T, total), 8), kListBlocks);
+        // recTile is free once the records are scattered: it holds the per-tile voxel sort
+        k_cv_tile_means<<<listGrid, 256, 0, s>>>(c->tileList.p, &c->dState.p->listCount, c->tileCount.p, c->rec.p,
+                                                 c->recTile.p, c->smask.p, c->spt.p, c->surfCount.p,
+                                                 &c->dState.p->surfaceTiles);
         if ((e = scan_ex(c->surfCount.p, c->surfCount.p, T, c->partial.p, s))) return cuda_fail(e, "surface scan");
-        k_cv_assign<<<warpBlocks, 256, 0, s>>>(c->smask.p, c->surfCount.p, T, c->spt.p, c->sslot.p, c->slots.p,
+        k_cv_assign<<<listGrid, 256, 0, s>>>(c->tileList.p, &c->dState.p->listCount, c->smask.p, c->surfCount.p, T,
+                                             c->spt.p, c->sslot.p, c->slots.p,
                                                c->dState.p);
-        k_cv_scanline<<<g.tilesY, 256, c->smemScan, s>>>(c->poly.p, n, g, c->inside.p, c->ovRows.p, c->dState.p);
-        k_cv_scanline_big<<<kBigBlocks, 1024, c->smemBig, s>>>(c->poly.p, n, g, c->inside.p, c->ovRows.p, c->dState.p);
+        k_cv_scanline<<<g.tilesY, 256, c->smemScan, s>>>(c->poly.p, n, rs, bk, g, c->inside.p, c->ovRows.p,
+                                                         c->dState.p);
+        k_cv_scanline_big<<<kBigBlocks, 1024, c->smemBig, s>>>(c->poly.p, n, rs, bk, g, c->inside.p, c->ovRows.p,
+                                                               c->dState.p);
         if ((e = cudaGetLastError())) return cuda_fail(e, "cv_rasterize launch");
     }
     if ((e = cudaEventRecord(c->ev1, s))) return cuda_fail(e, "event");
@@ -993,6 +1251,7 @@ int cv_stamp_disc(cv_canvas *c, float cx, float cy, float radius, int inside, cv
         (rc = c->nNew.reserve((size_t)nBox + 1)) || (rc = c->rimMask.reserve(nBox)) ||
         (rc = c->remMask.reserve(nBox)) || (rc = c->origMask.reserve(nBox)) ||
         (rc = c->rimPt.reserve((size_t)nBox * 64)) || (rc = c->partial.reserve((size_t)scan_partials(nBox + 1))) ||
+        (rc = c->tileList.reserve((size_t)std::min(nBox, n))) ||
         (rc = c->dirty.reserve((size_t)nBox * 64 + n)) || (rc = c->dirtyVal.reserve((size_t)nBox * 64 + n)) ||
         (rc = grow_keep(c->slots, (size_t)nslots + n, (size_t)nslots, s)) ||
         (rc = grow_keep(c->freel, (size_t)nslots + n, (size_t)c->st.nfree, s)))
@@ -1001,15 +1260,18 @@ int cv_stamp_disc(cv_canvas *c, float cx, float cy, float radius, int inside, cv
     if ((e = cudaMemcpyAsync(c->rimXY.p, c->rimHost.data(), sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, s)) ||
         (e = cudaMemsetAsync(&c->dState.p->removed, 0, 5 * sizeof(int), s)) ||
         (e = cudaMemsetAsync(&c->dState.p->err, 0, sizeof(int), s)) ||
+        (e = cudaMemsetAsync(&c->dState.p->listCount, 0, sizeof(int), s)) ||
+        (e = cudaMemsetAsync(c->rimMask.p, 0, sizeof(unsigned long long) * (size_t)nBox, s)) ||
         (e = cudaMemsetAsync(c->boxCount.p, 0, sizeof(int) * ((size_t)nBox + 1), s)))
         return cuda_fail(e, "cv_stamp_disc");
     k_cv_rim_bin<<<blocks_for(n, 256), 256, 0, s>>>(c->rimXY.p, p, g, c->inside.p, c->boxCount.p, c->recTile.p,
-                                                    c->recRank.p, c->dState.p);
+                                                    c->recRank.p, c->tileList.p, c->dState.p);
     if ((e = scan_ex(c->boxCount.p, c->boxCount.p, nBox, c->partial.p, s))) return cuda_fail(e, "rim scan");
     k_cv_scatter<<<blocks_for(n, 256), 256, 0, s>>>(n, c->recTile.p, c->recRank.p, c->rimXY.p, c->boxCount.p, g,
                                                     c->rec.p);
-    k_cv_tile_means<<<blocks_for(nBox, 256), 256, 0, s>>>(c->boxCount.p, nBox, c->rec.p, c->rimMask.p, c->rimPt.p,
-                                                          nullptr, nullptr);
+    k_cv_tile_means<<<std::min(blocks_for(std::min(nBox, n), 8), kListBlocks), 256, 0, s>>>(
+        c->tileList.p, &c->dState.p->listCount, c->boxCount.p, c->rec.p, c->recTile.p, c->rimMask.p, c->rimPt.p,
+        nullptr, nullptr);
     k_cv_stamp_tiles<<<blocks_for(nBox, 8), 256, 0, s>>>(p, g, nBox, c->inside.p, c->smask.p, c->spt.p, c->rimMask.p,
                                                          c->remMask.p, c->origMask.p, c->nRem.p, c->nRim.p,
                                                          c->nNew.p, c->dState.p);

@@ -44,6 +44,25 @@ def test_rasterize_bit_exact(vm, orc, name):
     c.close()
 
 
+@pytest.mark.parametrize("name", ["heart_1k", "comb", "odd_grid"])
+def test_rasterize_without_edge_buckets(vm, orc, monkeypatch, name):
+    """The scanline kernels' path that tests every edge (taken when the
+    per-row edge buckets would be too large) gives the same canvas."""
+    monkeypatch.setenv("VM_CANVAS_BUCKET_CAP", "0")
+    (w, h, vs), poly = next((d, p) for n, d, p in _shapes() if n == name)
+    c = vm.Canvas(w, h, vs)
+    c.RasterizeShape(poly)
+    o = orc.Canvas(w, h, vs)
+    o.rasterize(poly)
+    _same(c.state(), o.state(), orc)
+
+
+def test_rasterize_rejects_non_finite(vm):
+    c = vm.Canvas(8.0, 8.0, 1.0)
+    with pytest.raises(vm.VmError):
+        c.RasterizeShape(np.array([[1.0, 1.0], [np.nan, 2.0], [3.0, 5.0]], np.float32))
+
+
 def test_rasterize_empty_and_repeat(vm, orc):
     from voromesh_gb300 import synth
 
