@@ -33,6 +33,7 @@
 
 #include "vm_capi.h"
 #include "vm_host.h"
+#include "vm_kernels.h"
 
 using vmh::cuda_fail;
 using vmh::DevBuf;
@@ -1407,6 +1408,13 @@ int cv_is_inside(cv_canvas *c, int i, int j, int *out) { return cv_bit(c, c ? c-
 int cv_is_surface(cv_canvas *c, int i, int j, int *out) { return cv_bit(c, c ? c->smask.p : nullptr, i, j, out); }
 
 } // extern "C"
+
+cudaError_t vm_scan_ex(const int *in, int *out, int n, int *partial, cudaStream_t s)
+{
+    return scan_ex(in, out, n, partial, s);
+}
+
+int vm_scan_partials(int n) { return scan_partials(n); }
 
 // Internal view for the optimiser hand-off (vm_runtime.cu).
 namespace vmh {

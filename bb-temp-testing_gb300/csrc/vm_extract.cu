@@ -325,7 +325,128 @@ __global__ void __launch_bounds__(256) k_compact_cells(const float2 *__restrict_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Boundary assembly (reference voro_optimizer.cu:798-854) on the device.
+// Boundary edges are emitted in the reference's loop order (cell, then edge
+// within the cell); occurrence 2e / 2e+1 is edge e's first / second vertex.
+// A vertex is the sorted generator triple of its cell corner (labels + 4,
+// 21 bits each); vertices are numbered by first occurrence, as the
+// reference's insertion-ordered map numbers them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long triple_key(int a, int b, int c)
+{
+    unsigned long long v0 = (unsigned long long)(a + 4), v1 = (unsigned long long)(b + 4),
+                       v2 = (unsigned long long)(c + 4);
+    unsigned long long t;
+    if (v0 > v1) { t = v0; v0 = v1; v1 = t; }
+    if (v1 > v2) { t = v1; v1 = v2; v2 = t; }
+    if (v0 > v1) { t = v0; v0 = v1; v1 = t; }
+    return (v0 << 42) | (v1 << 21) | v2;
+}
+
+__device__ __forceinline__ bool boundary_edge(int l, const unsigned char *inside) { return !(l >= 0 && inside[l]); }
+
+__global__ void k_bnd_count(int n, const int *__restrict__ start, const int *__restrict__ labels,
+                            const unsigned char *__restrict__ inside, int *__restrict__ cnt)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int m = 0;
+    if (inside[i])
+        for (int k = start[i]; k < start[i + 1]; ++k) m += boundary_edge(labels[k], inside);
+    cnt[i] = m;
+}
+
+// Open-addressing insert of a vertex key; returns its slot. The table is at
+// least twice the number of occurrences, so a free slot is always reached.
+__device__ __forceinline__ unsigned bnd_insert(unsigned long long *keys, unsigned mask, unsigned long long key)
+{
+    unsigned long long h = key;
+    h ^= h >> 33; h *= 0xff51afd7ed558ccdULL; h ^= h >> 33; h *= 0xc4ceb9fe1a85ec53ULL; h ^= h >> 33;
+    unsigned s = (unsigned)h & mask;
+    for (unsigned probe = 0; probe <= mask; ++probe) {
+        unsigned long long old = atomicCAS(&keys[s], ~0ull, key);
+        if (old == ~0ull || old == key) return s;
+        s = (s + 1) & mask;
+    }
+    return 0xffffffffu; // unreachable at half load
+}
+
+__global__ void k_bnd_emit(int n, const int *__restrict__ start, const int *__restrict__ labels,
+                           const float2 *__restrict__ verts, const unsigned char *__restrict__ inside,
+                           const int *__restrict__ eStart, unsigned long long *__restrict__ keys, unsigned mask,
+                           int *__restrict__ minPos, unsigned *__restrict__ occSlot, float2 *__restrict__ occPt,
+                           int *__restrict__ err)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !inside[i]) return;
+    const int b = start[i], c = start[i + 1] - b;
+    int e = eStart[i];
+    for (int k = 0; k < c; ++k) {
+        const int l = labels[b + k];
+        if (!boundary_edge(l, inside)) continue;
+        const int prev = labels[b + (k + c - 1) % c], next = labels[b + (k + 1) % c];
+        const unsigned long long ka = triple_key(i, prev, l), kb = triple_key(i, l, next);
+        const unsigned sa = bnd_insert(keys, mask, ka), sb = bnd_insert(keys, mask, kb);
+        if (sa == 0xffffffffu || sb == 0xffffffffu) {
+            atomicOr(err, 1);
+            return;
+        }
+        atomicMin(&minPos[sa], 2 * e);
+        atomicMin(&minPos[sb], 2 * e + 1);
+        occSlot[2 * e] = sa;
+        occSlot[2 * e + 1] = sb;
+        occPt[2 * e] = verts[b + k];
+        occPt[2 * e + 1] = verts[b + (k + 1) % c];
+        ++e;
+    }
+}
+
+__global__ void k_bnd_first(int occ, const unsigned *__restrict__ occSlot, const int *__restrict__ minPos,
+                            int *__restrict__ first)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < occ) first[p] = minPos[occSlot[p]] == p;
+}
+
+// first[] now holds the exclusive scan of the first-occurrence flags
+__global__ void k_bnd_number(int occ, const unsigned *__restrict__ occSlot, const int *__restrict__ minPos,
+                             const int *__restrict__ first, const float2 *__restrict__ occPt, int *__restrict__ edges,
+                             float2 *__restrict__ vertices)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= occ) return;
+    const int f = minPos[occSlot[p]];
+    edges[p] = first[f];
+    if (f == p) vertices[first[p]] = occPt[p];
+}
+
 } // namespace vmk
+
+cudaError_t vm_launch_boundary(int n, const int *start, const int *labels, const float2 *verts,
+                               const unsigned char *inside, int *cnt, int phase, const int *eStart,
+                               unsigned long long *keys, unsigned mask, int *minPos, unsigned *occSlot, float2 *occPt,
+                               int occ, int *first, int *edges, float2 *vertices, int *err, cudaStream_t s)
+{
+    switch (phase) {
+    case 0:
+        if (n > 0) vmk::k_bnd_count<<<(n + 255) / 256, 256, 0, s>>>(n, start, labels, inside, cnt);
+        break;
+    case 1:
+        if (n > 0)
+            vmk::k_bnd_emit<<<(n + 255) / 256, 256, 0, s>>>(n, start, labels, verts, inside, eStart, keys, mask, minPos,
+                                                            occSlot, occPt, err);
+        break;
+    case 2:
+        if (occ > 0) vmk::k_bnd_first<<<(occ + 255) / 256, 256, 0, s>>>(occ, occSlot, minPos, first);
+        break;
+    default:
+        if (occ > 0)
+            vmk::k_bnd_number<<<(occ + 255) / 256, 256, 0, s>>>(occ, occSlot, minPos, first, occPt, edges, vertices);
+        break;
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t vm_launch_compact_cells(const float2 *verts, const int *labels, const int *start, int n, float2 *outV,
                                     int *outL, cudaStream_t s)

@@ -61,9 +61,9 @@ struct MeshHost {
     float gpuMs = 0.0f, hostMs = 0.0f;
 };
 
-// Boundary vertices, edges, watertightness and loops from the packed cells
-// (mesh.cellStart, cellVerts, cellLabels, inside).
-void assemble_boundary(int n, MeshHost &mesh);
+// Watertightness and loops of the boundary from mesh.edges / mesh.vertices
+// (the edges and vertices themselves are assembled on the device).
+void boundary_topology(MeshHost &mesh);
 
 // Device view of a canvas for the optimiser hand-off (vm_canvas.cu): its
 // target slots and occupancy, and the last edit's dirty slots, their values

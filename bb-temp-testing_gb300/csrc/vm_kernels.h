@@ -40,6 +40,19 @@ cudaError_t vm_launch_cells_n(const VmFit *fit, int nSlots, const unsigned long 
                               unsigned char *outInside, int *flags, cudaStream_t s);
 cudaError_t vm_launch_compact_cells(const float2 *verts, const int *labels, const int *start, int n, float2 *outV,
                                     int *outL, cudaStream_t s);
+// Boundary assembly on the device, in phases: 0 counts each inside cell's
+// boundary edges (cnt); 1 emits their vertex keys into the hash table
+// (keys/minPos, capacity mask + 1) with eStart = scanned counts; 2 flags the
+// first occurrences (first); after an exclusive scan of `first`, 3 numbers
+// the vertices and writes edges (2 per boundary edge) and vertex positions.
+cudaError_t vm_launch_boundary(int n, const int *start, const int *labels, const float2 *verts,
+                               const unsigned char *inside, int *cnt, int phase, const int *eStart,
+                               unsigned long long *keys, unsigned mask, int *minPos, unsigned *occSlot, float2 *occPt,
+                               int occ, int *first, int *edges, float2 *vertices, int *err, cudaStream_t s);
+// Exclusive scan of n ints (out[n] = total; in == out allowed); `partial`
+// holds vm_scan_partials(n) ints.
+cudaError_t vm_scan_ex(const int *in, int *out, int n, int *partial, cudaStream_t s);
+int vm_scan_partials(int n);
 
 // Poisson phase-grid sampler (vm_poisson.cu)
 struct PdParams {

@@ -42,56 +42,11 @@ int floor_log2f(float h)
     return e - 1;
 }
 
-// Boundary assembly of Extract() (reference voro_optimizer.cu:798-854).
-void assemble_boundary(int n, MeshHost &mesh)
+// Watertightness and loop count of the boundary (reference
+// voro_optimizer.cu:836-854) from its edges: watertight when every vertex
+// has exactly one outgoing and one incoming edge; loops = cycles then.
+void boundary_topology(MeshHost &mesh)
 {
-    const std::vector<uint8_t> &inside = mesh.inside;
-    auto count = [&](int i) { return mesh.cellStart[i + 1] - mesh.cellStart[i]; };
-    // vertex key: the sorted generator triple (labels offset by the 4 box sides, 21 bits each)
-    auto key = [](int a, int b, int c) {
-        uint64_t v0 = uint64_t(a + 4), v1 = uint64_t(b + 4), v2 = uint64_t(c + 4);
-        if (v0 > v1) std::swap(v0, v1);
-        if (v1 > v2) std::swap(v1, v2);
-        if (v0 > v1) std::swap(v0, v1);
-        return (v0 << 42) | (v1 << 21) | v2;
-    };
-    size_t maxEdges = 0;
-    for (int i = 0; i < n; ++i)
-        if (inside[i]) maxEdges += (size_t)count(i);
-    size_t cap = 64;
-    while (cap < 4 * (maxEdges + 16)) cap <<= 1;
-    std::vector<uint64_t> keys(cap);
-    std::vector<int> vals(cap, -1);
-    auto vertex = [&](uint64_t k, float2 p) {
-        uint64_t h = k;
-        h ^= h >> 33; h *= 0xff51afd7ed558ccdULL; h ^= h >> 33; h *= 0xc4ceb9fe1a85ec53ULL; h ^= h >> 33;
-        size_t s = (size_t)h & (cap - 1);
-        while (vals[s] >= 0) {
-            if (keys[s] == k) return vals[s];
-            s = (s + 1) & (cap - 1);
-        }
-        keys[s] = k;
-        vals[s] = (int)mesh.vertices.size();
-        mesh.vertices.push_back(p);
-        return vals[s];
-    };
-    mesh.vertices.clear();
-    mesh.edges.clear();
-    for (int i = 0; i < n; ++i) {
-        if (!inside[i]) continue;
-        int c = count(i);
-        const int *lab = mesh.cellLabels.data() + mesh.cellStart[i];
-        const float2 *pos = mesh.cellVerts.data() + mesh.cellStart[i];
-        for (int k = 0; k < c; ++k) {
-            int l = lab[k];
-            if (l >= 0 && inside[l]) continue;
-            int prev = lab[(k + c - 1) % c], next = lab[(k + 1) % c];
-            int a = vertex(key(i, prev, l), pos[k]);
-            int b = vertex(key(i, l, next), pos[(k + 1) % c]);
-            mesh.edges.push_back(a);
-            mesh.edges.push_back(b);
-        }
-    }
     size_t nv = mesh.vertices.size(), ne = mesh.edges.size() / 2;
     std::vector<int> nxt(nv, -1), inDeg(nv, 0);
     mesh.watertight = true;
@@ -154,6 +109,10 @@ struct vm_optimizer {
     DevBuf<VmFit> dFit;
     DevBuf<VmPointSet> dSites, dTargets, dCsrSet;
     DevBuf<int> cellStartD, csrTiles, csrLabels, dCsrPre; // extraction: cells packed in CSR order
+    DevBuf<int> bndCnt, bndPartial, bndErr, bndMin, bndFirst, bndEdges; // boundary assembly
+    DevBuf<unsigned long long> bndKeys;
+    DevBuf<unsigned> bndSlot;
+    DevBuf<float2> bndPt, bndVerts;
     DevBuf<float2> csrVerts;
     DevBuf<int> dPre; // [0, siteBlocks, 0, tiles, 0, lossTiles, 0, targetBlocks]
     DevBuf<int> dTPre; // [0, targetBlocks, 0, targetKeyTiles]
@@ -1028,7 +987,7 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
         return rc;
     C.start = h->cellStartD.p;
     C.tileSums = h->csrTiles.p;
-    int total = 0, flags[2];
+    int total = 0, flags[2], nBnd = 0, nVert = 0;
     if ((e = cudaMemcpyAsync(h->dCsrSet.p, &C, sizeof(C), cudaMemcpyHostToDevice, h->stream)) ||
         (e = cudaMemcpyAsync(h->dCsrPre.p, pre, sizeof(pre), cudaMemcpyHostToDevice, h->stream)) ||
         (e = vm_launch_scan(h->dCsrSet.p, h->dCsrPre.p, 1, tiles, h->stream)) ||
@@ -1039,6 +998,45 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
     if ((e = vm_launch_compact_cells(h->cellVerts.p, h->cellEdges.p, h->cellStartD.p, n, h->csrVerts.p,
                                      h->csrLabels.p, h->stream)))
         return cuda_fail(e, "extract pack");
+    // boundary assembly on the device (reference voro_optimizer.cu:798-835):
+    // boundary edges in cell order, vertices numbered by first occurrence
+    if ((rc = h->bndCnt.reserve((size_t)n + 1)) || (rc = h->bndPartial.reserve((size_t)vm_scan_partials(n + 1))) ||
+        (rc = h->bndErr.reserve(1)))
+        return rc;
+    if ((e = cudaMemsetAsync(h->bndErr.p, 0, sizeof(int), h->stream)) ||
+        (e = vm_launch_boundary(n, h->cellStartD.p, h->csrLabels.p, h->csrVerts.p, h->inside.p, h->bndCnt.p, 0, nullptr,
+                                nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr,
+                                h->stream)) ||
+        (e = vm_scan_ex(h->bndCnt.p, h->bndCnt.p, n, h->bndPartial.p, h->stream)) ||
+        (e = cudaMemcpyAsync(&nBnd, h->bndCnt.p + n, sizeof(int), cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaStreamSynchronize(h->stream)))
+        return cuda_fail(e, "boundary count");
+    const int occ = 2 * nBnd;
+    if (occ > 0) {
+        size_t cap = 64;
+        while (cap < 2 * (size_t)occ) cap <<= 1;
+        if ((rc = h->bndKeys.reserve(cap)) || (rc = h->bndMin.reserve(cap)) || (rc = h->bndSlot.reserve(occ)) ||
+            (rc = h->bndPt.reserve(occ)) || (rc = h->bndFirst.reserve((size_t)occ + 1)) ||
+            (rc = h->bndEdges.reserve(occ)) || (rc = h->bndVerts.reserve(occ)) ||
+            (rc = h->bndPartial.reserve((size_t)vm_scan_partials(occ + 1))))
+            return rc;
+        unsigned mask = (unsigned)(cap - 1);
+        if ((e = cudaMemsetAsync(h->bndKeys.p, 0xFF, cap * sizeof(unsigned long long), h->stream)) ||
+            (e = cudaMemsetAsync(h->bndMin.p, 0x7F, cap * sizeof(int), h->stream)) ||
+            (e = vm_launch_boundary(n, h->cellStartD.p, h->csrLabels.p, h->csrVerts.p, h->inside.p, nullptr, 1,
+                                    h->bndCnt.p, h->bndKeys.p, mask, h->bndMin.p, h->bndSlot.p, h->bndPt.p, occ,
+                                    nullptr, nullptr, nullptr, h->bndErr.p, h->stream)) ||
+            (e = vm_launch_boundary(n, nullptr, nullptr, nullptr, nullptr, nullptr, 2, nullptr, nullptr, mask,
+                                    h->bndMin.p, h->bndSlot.p, nullptr, occ, h->bndFirst.p, nullptr, nullptr, nullptr,
+                                    h->stream)) ||
+            (e = vm_scan_ex(h->bndFirst.p, h->bndFirst.p, occ, h->bndPartial.p, h->stream)) ||
+            (e = vm_launch_boundary(n, nullptr, nullptr, nullptr, nullptr, nullptr, 3, nullptr, nullptr, mask,
+                                    h->bndMin.p, h->bndSlot.p, h->bndPt.p, occ, h->bndFirst.p, h->bndEdges.p,
+                                    h->bndVerts.p, nullptr, h->stream)) ||
+            (e = cudaMemcpyAsync(&nVert, h->bndFirst.p + occ, sizeof(int), cudaMemcpyDeviceToHost, h->stream)) ||
+            (e = cudaStreamSynchronize(h->stream)))
+            return cuda_fail(e, "boundary assembly");
+    }
     MeshHost &M = h->mesh;
     M.generators.resize(n);
     M.inside.resize(n);
@@ -1050,12 +1048,22 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
         (total && (e = cudaMemcpyAsync(M.cellLabels.data(), h->csrLabels.p, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, h->stream))) ||
         (e = cudaMemcpyAsync(M.inside.data(), h->inside.p, n, cudaMemcpyDeviceToHost, h->stream)) ||
         (e = cudaMemcpyAsync(M.generators.data(), h->gen.p, sizeof(float2) * n, cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(flags, h->flags.p, sizeof(flags), cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(flags, h->flags.p, sizeof(flags), cudaMemcpyDeviceToHost, h->stream)))
+        return cuda_fail(e, "extract read");
+    M.edges.resize((size_t)occ);
+    M.vertices.resize((size_t)nVert);
+    int bndErr = 0;
+    if ((occ && (e = cudaMemcpyAsync(M.edges.data(), h->bndEdges.p, sizeof(int) * (size_t)occ, cudaMemcpyDeviceToHost,
+                                     h->stream))) ||
+        (nVert && (e = cudaMemcpyAsync(M.vertices.data(), h->bndVerts.p, sizeof(float2) * (size_t)nVert,
+                                       cudaMemcpyDeviceToHost, h->stream))) ||
+        (e = cudaMemcpyAsync(&bndErr, h->bndErr.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream)) ||
         (e = cudaStreamSynchronize(h->stream)))
         return cuda_fail(e, "extract read");
+    if (bndErr) return fail(VM_ERR_CUDA, "boundary assembly: vertex table full");
     M.unsafeCells = flags[0];
     M.overflowCells = flags[1];
-    assemble_boundary(n, M);
+    boundary_topology(M);
     M.hostMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     info->numGenerators = n;
     info->numCellVerts = (int)M.cellVerts.size();

@@ -142,3 +142,38 @@ def test_uncertified_cells(vm, orc):
     gen = np.ascontiguousarray(np.concatenate([dense, sparse]))
     mesh = run_case(vm, orc, gen, 0.02)
     assert mesh.unsafeCells > 0
+
+
+@pytest.mark.parametrize("n,jitter", [(3000, None), (48 * 48, 1e-3), (60000, None)])
+def test_boundary_assembly_bit_exact(vm, orc, n, jitter):
+    """The device boundary assembly (vertex keys, first-seen numbering, edges,
+    watertightness, loops) equals the oracle's restatement of
+    voro_optimizer.cu:798-854 run on the same cells, bit for bit."""
+    from voromesh_gb300 import OptimizerParams, VoroOptimizer, synth
+
+    if jitter is None:
+        gen = synth.uniform(41, 1, n)
+        gen[::17] = -1.0
+        spacing = float(2.0 / np.sqrt(n))
+    else:
+        gen = synth.lattice(7, 7, 48, 48, jitter)
+        spacing = 2.0 / 48
+    masks, tiles, voxel = disc_masks()
+    opt = VoroOptimizer(2.0, 2.0, spacing, OptimizerParams(lossK=12))
+    opt.SetTargets(gen[:8])
+    opt.SetOccupancy(masks, tiles, tiles, voxel)
+    opt.SetGenerators(gen, len(gen), 1, 2.0)
+    m = opt.Extract()
+    counts = np.diff(m.cellStart).astype(np.int32)
+    K = 24
+    verts = np.zeros((len(gen), K, 2), np.float32)
+    labels = np.zeros((len(gen), K), np.int32)
+    for i in range(len(gen)):
+        a, b = m.cellStart[i], m.cellStart[i + 1]
+        verts[i, :b - a] = m.cellVerts[a:b]
+        labels[i, :b - a] = m.cellLabels[a:b]
+    _, mv, me, wt, loops = orc.assemble(verts, labels, counts, m.inside)
+    assert np.array_equal(m.edges, me)
+    assert np.array_equal(m.vertices.view(np.uint32), mv.view(np.uint32))
+    assert m.watertight == wt and m.loops == loops
+    assert len(me) > 0
