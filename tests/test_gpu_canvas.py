@@ -57,6 +57,26 @@ def test_rasterize_without_edge_buckets(vm, orc, monkeypatch, name):
     _same(c.state(), o.state(), orc)
 
 
+def test_rasterize_crossing_limit(vm, orc):
+    """A scanline crossed by more than 32768 edges is reported as unsupported
+    (status 7) without touching the device state beyond this call; one just
+    under the limit (block-per-row path) still matches the oracle."""
+    from voromesh_gb300 import synth
+
+    c = vm.Canvas(131072.0, 16.0, 1.0)
+    with pytest.raises(vm.VmError) as err:
+        c.RasterizeShape(synth.comb(1.0, 2.0, 131000.0, 10.0, 17000))
+    assert err.value.code == 7
+    c.close()
+    poly = synth.comb(1.0, 2.0, 60000.0, 10.0, 8000)  # 16000 crossings
+    c = vm.Canvas(65536.0, 16.0, 1.0)
+    c.RasterizeShape(poly)
+    o = orc.Canvas(65536.0, 16.0, 1.0)
+    o.rasterize(poly)
+    assert np.array_equal(c.InsideMasks(), o.inside())
+    assert np.array_equal(c.TargetSlots().view(np.uint32), o.slots().view(np.uint32))
+
+
 def test_rasterize_rejects_non_finite(vm):
     c = vm.Canvas(8.0, 8.0, 1.0)
     with pytest.raises(vm.VmError):
