@@ -282,6 +282,7 @@ size_t vmb_fit_bytes(int slotsW, int slotsH, int nTargets, float width, float he
 
 int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
 {
+    vmh::NvtxRange range("vmb_add_fit");
     if (!b || !in || !fitId) return fail(VM_ERR_ARG, "vmb_add_fit: bad arguments");
     *fitId = -1;
     int n = in->slotsW * in->slotsH;
@@ -474,6 +475,7 @@ int vmb_set_active(vmb_batch *b, int fitId, int active)
 
 int vmb_step(vmb_batch *b, int iterations, float *gpuMs)
 {
+    vmh::NvtxRange range("vmb_step");
     if (!b || iterations < 0) return fail(VM_ERR_ARG, "vmb_step: bad arguments");
     if (gpuMs) *gpuMs = 0.0f;
     int rc;
@@ -577,6 +579,7 @@ extern "C" {
 
 int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result *res)
 {
+    vmh::NvtxRange range("vms_serve");
     if (n < 0 || (n && (!reqs || !res)) || !cfg || cfg->stepsPerRound < 1 || cfg->maxLive < 1)
         return fail(VM_ERR_ARG, "vms_serve: bad arguments");
     vmb_batch *b = nullptr;

@@ -1124,6 +1124,7 @@ int cv_destroy(cv_canvas *c)
 
 int cv_rasterize(cv_canvas *c, const float *xy, int n, float *gpuMs)
 {
+    vmh::NvtxRange range("cv_rasterize");
     if (!c || n < 0 || (n > 0 && !xy)) return fail(VM_ERR_ARG, "cv_rasterize: bad arguments");
     for (long long k = 0; k < 2LL * n; ++k)
         if (!std::isfinite(xy[k])) return fail(VM_ERR_ARG, "cv_rasterize: polygon coordinates must be finite");
@@ -1212,6 +1213,7 @@ int cv_rasterize(cv_canvas *c, const float *xy, int n, float *gpuMs)
 
 int cv_stamp_disc(cv_canvas *c, float cx, float cy, float radius, int inside, cv_edit *out)
 {
+    vmh::NvtxRange range("cv_stamp_disc");
     if (!c || !out) return fail(VM_ERR_ARG, "cv_stamp_disc: bad arguments");
     *out = cv_edit{};
     c->lastEdit = cv_edit{};

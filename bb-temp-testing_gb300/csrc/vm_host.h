@@ -14,6 +14,15 @@ namespace vmh {
 
 constexpr int kMaxCellVerts = 24;
 
+// NVTX range over a public entry point (visible in Nsight timelines; no cost
+// without a profiler attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name);
+    ~NvtxRange();
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 int floor_log2f(float h);

@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "vm_capi.h"
 #include "vm_host.h"
 #include "vm_kernels.h"
@@ -20,6 +22,9 @@
 namespace vmh {
 
 thread_local std::string g_lastError;
+
+NvtxRange::NvtxRange(const char *name) { nvtxRangePushA(name); }
+NvtxRange::~NvtxRange() { nvtxRangePop(); }
 
 int fail(int code, const std::string &msg)
 {
@@ -540,12 +545,14 @@ static int set_targets_from(vm_optimizer *h, const void *xy, int n, cudaMemcpyKi
 
 int vm_set_targets(vm_optimizer *h, const float *xy, int n)
 {
+    vmh::NvtxRange range("vm_set_targets");
     if (!h || n < 0 || (n > 0 && !xy)) return fail(VM_ERR_ARG, "vm_set_targets: bad arguments");
     return set_targets_from(h, xy, n, cudaMemcpyHostToDevice);
 }
 
 int vm_update_targets(vm_optimizer *h, const int *dirty, int ndirty, const float *slots, int nslots)
 {
+    vmh::NvtxRange range("vm_update_targets");
     if (!h || ndirty < 0 || nslots < 0) return fail(VM_ERR_ARG, "vm_update_targets: bad arguments");
     if (ndirty == 0) return VM_OK;
     if (!dirty || !slots) return fail(VM_ERR_ARG, "vm_update_targets: NULL buffer");
@@ -610,6 +617,7 @@ int vm_update_occupancy(vm_optimizer *h, const uint64_t *masks, int tx0, int ty0
 
 int vm_set_generators(vm_optimizer *h, const float *xy, int slotsW, int slotsH, float slotCellSize)
 {
+    vmh::NvtxRange range("vm_set_generators");
     if (!h || slotsW < 0 || slotsH < 0) return fail(VM_ERR_ARG, "vm_set_generators: bad arguments");
     long long n64 = (long long)slotsW * slotsH;
     if (n64 > 0x7FFFFFFF / kMaxCellVerts) return fail(VM_ERR_ARG, "too many generator slots");
@@ -660,6 +668,7 @@ int vm_update_generators(vm_optimizer *h, const float *xy, int cx0, int cy0, int
 
 int vm_begin_schedule(vm_optimizer *h, int iterations, int cx0, int cy0, int cx1, int cy1)
 {
+    vmh::NvtxRange range("vm_begin_schedule");
     if (!h) return fail(VM_ERR_ARG, "NULL handle");
     cx0 = std::max(cx0, 0), cy0 = std::max(cy0, 0);
     cx1 = std::min(cx1, h->slotsW), cy1 = std::min(cy1, h->slotsH);
@@ -697,6 +706,7 @@ int vm_begin_schedule(vm_optimizer *h, int iterations, int cx0, int cy0, int cx1
 
 int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
 {
+    vmh::NvtxRange range("vm_step");
     if (!h) return fail(VM_ERR_ARG, "NULL handle");
     if (gpuMs) *gpuMs = 0.0f;
     if (iterations <= 0 || h->numSlots() == 0 || h->targetCapacity == 0) return VM_OK;
@@ -726,6 +736,7 @@ int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
 
 int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
 {
+    vmh::NvtxRange range("vm_step_timed");
     if (!h || !stageMs || iterations < 0) return fail(VM_ERR_ARG, "bad arguments");
     for (int k = 0; k < 4; ++k) stageMs[k] = 0.0f;
     if (iterations == 0 || h->numSlots() == 0 || h->targetCapacity == 0) return VM_OK;
@@ -792,6 +803,7 @@ int vm_get_loss_variant(vm_optimizer *h, int *variant, int *count)
 
 int vm_evaluate_loss(vm_optimizer *h, float *loss)
 {
+    vmh::NvtxRange range("vm_evaluate_loss");
     if (!h || !loss) return fail(VM_ERR_ARG, "bad arguments");
     *loss = 0.0f;
     if (h->numSlots() == 0 || h->targetCapacity == 0) return VM_OK;
@@ -955,6 +967,7 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
 
 int vm_extract(vm_optimizer *h, vm_mesh_info *info)
 {
+    vmh::NvtxRange range("vm_extract");
     if (!h || !info) return fail(VM_ERR_ARG, "bad arguments");
     std::memset(info, 0, sizeof(*info));
     h->mesh = MeshHost();
@@ -1094,10 +1107,64 @@ int vm_mesh_copy(vm_optimizer *h, float *generators, uint8_t *inside, int *cellS
 }
 
 // ===========================================================================
+// checkpoint / resume
+// ===========================================================================
+int vm_checkpoint(vm_optimizer *h, vm_checkpoint_info *info, float *gen, float *m, float *v)
+{
+    if (!h || !info) return fail(VM_ERR_ARG, "vm_checkpoint: bad arguments");
+    vmh::NvtxRange range("vm_checkpoint");
+    info->slotsW = h->slotsW;
+    info->slotsH = h->slotsH;
+    info->slotCellSize = h->slotCellSize;
+    info->scheduleLength = h->scheduleLength;
+    info->iteration = h->iteration;
+    info->cx0 = h->fit.cx0;
+    info->cy0 = h->fit.cy0;
+    info->cx1 = h->fit.cx1;
+    info->cy1 = h->fit.cy1;
+    info->lastBatchLoss = h->lastBatchLoss;
+    size_t bytes = sizeof(float2) * (size_t)h->numSlots();
+    cudaError_t e = cudaSuccess;
+    if (bytes && gen) e = cudaMemcpyAsync(gen, h->gen.p, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (!e && bytes && m) e = cudaMemcpyAsync(m, h->m.p, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (!e && bytes && v) e = cudaMemcpyAsync(v, h->v.p, bytes, cudaMemcpyDeviceToHost, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    return e ? cuda_fail(e, "vm_checkpoint") : VM_OK;
+}
+
+int vm_restore(vm_optimizer *h, const vm_checkpoint_info *info, const float *gen, const float *m, const float *v)
+{
+    if (!h || !info || info->iteration < 0 || info->scheduleLength < 0 ||
+        ((long long)info->slotsW * info->slotsH > 0 && (!gen || !m || !v)))
+        return fail(VM_ERR_ARG, "vm_restore: bad arguments");
+    vmh::NvtxRange range("vm_restore");
+    int rc;
+    if ((rc = vm_set_generators(h, gen, info->slotsW, info->slotsH, info->slotCellSize)) ||
+        (rc = vm_begin_schedule(h, info->scheduleLength, info->cx0, info->cy0, info->cx1, info->cy1)))
+        return rc;
+    size_t bytes = sizeof(float2) * (size_t)h->numSlots();
+    cudaError_t e = cudaSuccess;
+    if (bytes) {
+        e = cudaMemcpyAsync(h->m.p, m, bytes, cudaMemcpyHostToDevice, h->stream);
+        if (!e) e = cudaMemcpyAsync(h->v.p, v, bytes, cudaMemcpyHostToDevice, h->stream);
+    }
+    // the step counter drives the learning-rate milestones, the bias
+    // corrections and the subsample mask of the next steps
+    int iter = info->iteration;
+    if (!e) e = cudaMemcpyAsync(&h->state.p->iter, &iter, sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    if (e) return cuda_fail(e, "vm_restore");
+    h->iteration = info->iteration;
+    h->lastBatchLoss = info->lastBatchLoss;
+    return VM_OK;
+}
+
+// ===========================================================================
 // canvas hand-off (device to device)
 // ===========================================================================
 int vm_set_targets_from_canvas(vm_optimizer *h, cv_canvas *c)
 {
+    vmh::NvtxRange range("vm_set_targets_from_canvas");
     if (!h || !c) return fail(VM_ERR_ARG, "vm_set_targets_from_canvas: NULL handle");
     CanvasView v{};
     int rc;
@@ -1121,6 +1188,7 @@ int vm_set_targets_from_canvas(vm_optimizer *h, cv_canvas *c)
 
 int vm_update_from_canvas(vm_optimizer *h, cv_canvas *c)
 {
+    vmh::NvtxRange range("vm_update_from_canvas");
     if (!h || !c) return fail(VM_ERR_ARG, "vm_update_from_canvas: NULL handle");
     CanvasView v{};
     int rc;
@@ -1225,6 +1293,7 @@ int pd_destroy(pd_sampler *s)
 
 int pd_resample(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, float *gpuMs)
 {
+    vmh::NvtxRange range("pd_resample");
     if (!s) return fail(VM_ERR_ARG, "NULL sampler");
     if (gpuMs) *gpuMs = 0.0f;
     int x0 = std::max(cx0, 0), y0 = std::max(cy0, 0), x1 = std::min(cx1, s->gridW), y1 = std::min(cy1, s->gridH);
@@ -1250,6 +1319,7 @@ int pd_resample(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, float *gpuMs)
 
 int pd_resample_many(pd_sampler *const *samplers, const int *regions, int n, float *gpuMs)
 {
+    vmh::NvtxRange range("pd_resample_many");
     if (gpuMs) *gpuMs = 0.0f;
     if (n < 0 || (n && (!samplers || !regions))) return fail(VM_ERR_ARG, "pd_resample_many: bad arguments");
     for (int i = 0; i < n; ++i) {

@@ -50,6 +50,12 @@ class vm_mesh_info(C.Structure):
                 ("overflowCells", C.c_int), ("gpuMs", C.c_float), ("hostMs", C.c_float)]
 
 
+class vm_checkpoint_info(C.Structure):
+    _fields_ = [("slotsW", C.c_int), ("slotsH", C.c_int), ("slotCellSize", C.c_float), ("scheduleLength", C.c_int),
+                ("iteration", C.c_int), ("cx0", C.c_int), ("cy0", C.c_int), ("cx1", C.c_int), ("cy1", C.c_int),
+                ("lastBatchLoss", C.c_float)]
+
+
 class cv_edit(C.Structure):
     _fields_ = [("tx0", C.c_int), ("ty0", C.c_int), ("tx1", C.c_int), ("ty1", C.c_int), ("removed", C.c_int),
                 ("added", C.c_int), ("flipped", C.c_int), ("ndirty", C.c_int)]
@@ -122,6 +128,8 @@ SIGNATURES = {
     "cv_is_inside": [P, I, I, P],
     "cv_is_surface": [P, I, I, P],
     "vm_set_targets_from_canvas": [P, P],
+    "vm_checkpoint": [P, P, P, P, P],
+    "vm_restore": [P, P, P, P, P],
     "vm_update_from_canvas": [P, P],
     # seeded generators (host only)
     "vm_synth_uniform": [C.c_uint64, C.c_uint64, C.c_int64, C.c_double, C.c_double, I, P],

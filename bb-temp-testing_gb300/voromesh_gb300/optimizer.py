@@ -12,7 +12,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import check, load, pd_info_t, ptr, vm_info_t, vm_mesh_info, vm_params
+from ._lib import check, load, pd_info_t, ptr, vm_checkpoint_info, vm_info_t, vm_mesh_info, vm_params
 
 
 def _pts(a, name: str) -> np.ndarray:
@@ -114,6 +114,24 @@ class VoroOptimizer:
     def UpdateOccupancy(self, masks, tx0: int, ty0: int, tx1: int, ty1: int) -> None:
         m = np.ascontiguousarray(masks, dtype=np.uint64)
         check(self._lib.vm_update_occupancy(self._h, ptr(m), tx0, ty0, tx1, ty1), "UpdateOccupancy")
+
+    # ---- checkpoint / resume (GB300 extension) ----
+    def Checkpoint(self) -> dict:
+        """The fit's optimisation state: slot layout, schedule, step counter,
+        last batch loss, generators and Adam moments."""
+        info = vm_checkpoint_info()
+        check(self._lib.vm_checkpoint(self._h, C.byref(info), None, None, None), "Checkpoint")
+        n = info.slotsW * info.slotsH
+        g, m, v = (np.empty((n, 2), np.float32) for _ in range(3))
+        check(self._lib.vm_checkpoint(self._h, C.byref(info), ptr(g), ptr(m), ptr(v)), "Checkpoint")
+        return {"info": {k: getattr(info, k) for k, _ in vm_checkpoint_info._fields_}, "generators": g, "m": m, "v": v}
+
+    def Restore(self, ckpt: dict) -> None:
+        """Resumes a Checkpoint() in an optimiser made with the same arguments,
+        targets and occupancy: the next Step continues the saved run."""
+        info = vm_checkpoint_info(**ckpt["info"])
+        g, m, v = (np.ascontiguousarray(ckpt[k], np.float32) for k in ("generators", "m", "v"))
+        check(self._lib.vm_restore(self._h, C.byref(info), ptr(g), ptr(m), ptr(v)), "Restore")
 
     # ---- device-to-device hand-off from a Canvas (GB300 extension) ----
     def SetTargetsFromCanvas(self, canvas) -> None:

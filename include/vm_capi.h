@@ -134,6 +134,26 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info);
 int vm_mesh_copy(vm_optimizer *h, float *generators, uint8_t *inside, int *cellStart, float *cellVerts,
                  float *vertices, int *edges, int *cellLabels);
 
+/* ---- checkpoint / resume (no counterpart in the reference) -------------------- */
+/* The optimisation state of a fit, beside its generators and Adam moments:
+ * the slot layout, the current schedule (BeginSchedule's length and slot
+ * rectangle), the step counter and the last batch loss. */
+typedef struct {
+    int slotsW, slotsH;
+    float slotCellSize;
+    int scheduleLength, iteration;
+    int cx0, cy0, cx1, cy1;
+    float lastBatchLoss;
+} vm_checkpoint_info;
+/* Snapshot: info plus numSlots (x, y) pairs each of generators, m and v (any
+ * array may be NULL). */
+int vm_checkpoint(vm_optimizer *h, vm_checkpoint_info *info, float *gen, float *m, float *v);
+/* Resume into an optimiser made with the same constructor arguments and the
+ * same targets and occupancy: SetGenerators + BeginSchedule of the saved
+ * schedule, then the saved moments and step counter. The next Step continues
+ * the saved run bit for bit. */
+int vm_restore(vm_optimizer *h, const vm_checkpoint_info *info, const float *gen, const float *m, const float *v);
+
 /* ---- inspection (used by the parity tests) ----------------------------------- */
 /* The hash grid of the current generators: start (gridW*gridH+1), sortedIdx and
  * sortedPos (live sites, cell order, ascending slot within a cell), genCell (numSlots). */
