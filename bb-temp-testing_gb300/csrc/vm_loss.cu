@@ -801,13 +801,16 @@ static void *variant_fn(int v)
 cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode,
                            int gridBlocks, int variant, void *queue, cudaStream_t s)
 {
-    if (totalTiles <= 0) return cudaSuccess;
-    int g = gridBlocks < totalTiles ? gridBlocks : totalTiles;
-    if (g < 1) g = 1;
     SlowQueue *q = static_cast<SlowQueue *>(queue);
-    void *args[] = {(void *)&fits, (void *)&tilePrefix, (void *)&nFits, (void *)&mode, (void *)&q};
-    cudaError_t e = cudaLaunchKernel(variant_fn(variant), dim3(g), dim3(vm_loss_variant_threads(variant)), args, 0, s);
-    if (e) return e;
+    if (totalTiles > 0) {
+        int g = gridBlocks < totalTiles ? gridBlocks : totalTiles;
+        if (g < 1) g = 1;
+        void *args[] = {(void *)&fits, (void *)&tilePrefix, (void *)&nFits, (void *)&mode, (void *)&q};
+        cudaError_t e =
+            cudaLaunchKernel(variant_fn(variant), dim3(g), dim3(vm_loss_variant_threads(variant)), args, 0, s);
+        if (e) return e;
+    }
+    // with no targets the step still needs its Adam schedule (k_loss_exact)
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -177,3 +177,26 @@ def test_checkpoint_resume_bit_exact(vm, fraction, rect):
     mb, vb = b.Moments()
     assert np.array_equal(ma, mb) and np.array_equal(va, vb)
     assert a.LastBatchLoss() == b.LastBatchLoss() and a.Iteration() == b.Iteration()
+
+
+def test_steps_after_every_target_is_removed(vm, orc):
+    """With no live targets the step still follows the Adam schedule: the
+    moments decay and the sites keep moving as the oracle's do."""
+    from voromesh_gb300 import synth
+
+    gen = synth.uniform(6, 1, 512)
+    tgt = synth.circle(6, 2, 4096, 0.6, 1e-3)
+    opt, ref = _pair(vm, orc, gen, tgt, 0.1, 12, 0, 1.0, iters=40)
+    opt.Step(8)
+    ref.step(8)
+    empty = np.full_like(tgt, -1.0)
+    opt.UpdateTargets(np.arange(len(tgt)), empty)
+    ref.set_targets(empty)
+    for _ in range(3):
+        opt.Step(4)
+        ref.step(4)
+        g, m, v = ref.generators()
+        assert np.array_equal(opt.Generators(), g)
+        om, ov = opt.Moments()
+        assert np.array_equal(om, m) and np.array_equal(ov, v)
+    assert opt.info().liveTargets == 0
