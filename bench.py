@@ -284,8 +284,9 @@ def run_batch(args):
 
 
 def run_extract(args):
-    """Mesh extraction: the Voronoi-cell clipper (GPU) and the packing plus
-    boundary assembly (host) on the 1M-site fit after 50 steps, and on the
+    """Mesh extraction: the Voronoi-cell clipper (GPU) and the CSR packing,
+    boundary assembly (both on the GPU) and copy-out to the host
+    (host_assembly_ms) on the 1M-site fit after 50 steps, and on the
     512x512 lattice with 1e-6 jitter (near-cocircular bisectors); occupancy is
     a disc of radius 0.6 at the domain centre on a half-spacing voxel grid.
     cells/s = sites / clipper GPU time."""
