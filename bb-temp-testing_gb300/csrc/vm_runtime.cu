@@ -973,6 +973,9 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
     h->mesh = MeshHost();
     int n = h->numSlots();
     if (n == 0) return VM_OK;
+    // boundary vertex keys hold three 21-bit fields (label + 4), as in the
+    // reference (voro_optimizer.cu:809-815): larger meshes would merge vertices
+    if (n > (1 << 21) - 4) return fail(VM_ERR_UNSUPPORTED, "vm_extract: more than 2^21 - 4 generator slots");
     int rc;
     if ((rc = h->cellVerts.reserve((size_t)n * kMaxCellVerts)) || (rc = h->cellEdges.reserve((size_t)n * kMaxCellVerts)) ||
         (rc = h->cellCount.reserve(n)) || (rc = h->inside.reserve(n)))
