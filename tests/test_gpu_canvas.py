@@ -31,6 +31,16 @@ def _shapes():
     # sample-order fallback of the per-voxel sums
     yield "tiny_coords", (8.0, 8.0, 1.0), np.array([[1e-30, 0.25], [0.75, 1e-25], [0.9, 0.9], [3.0, 7.0]], np.float32)
     yield "single_vertex", (8.0, 8.0, 1.0), np.array([[3.5, 4.25]], np.float32)
+    # vertices on voxel centres and boundaries, a horizontal edge, a repeated vertex
+    yield "grid_aligned", (32.0, 32.0, 1.0), np.array(
+        [[4.5, 4.5], [20, 4.5], [20, 4.5], [20, 10], [27.5, 10], [27.5, 27.5], [4, 27.5], [4, 16], [10.5, 16],
+         [10.5, 12], [4.5, 12]], np.float32)
+    # self-intersecting (even-odd fill) and clockwise outlines, a near-degenerate sliver
+    t = np.arange(5) * 4 * np.pi / 5 - np.pi / 2
+    yield "pentagram", (64.0, 64.0, 1.0), np.stack([32 + 25 * np.cos(t), 32 + 25 * np.sin(t)], 1).astype(np.float32)
+    yield "clockwise_square", (16.0, 16.0, 0.5), np.array([[2, 2], [2, 12], [12, 12], [12, 2]], np.float32)
+    yield "sliver", (16.0, 16.0, 1.0), np.array([[1, 8], [15, 8.0001], [15, 8.0002], [1, 8.0003]], np.float32)
+    yield "random_poly", (50.0, 40.0, 0.7), np.random.default_rng(3).uniform(-5, 55, (40, 2)).astype(np.float32)
 
 
 @pytest.mark.parametrize("name", [s[0] for s in _shapes()])
