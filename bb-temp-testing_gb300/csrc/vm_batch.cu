@@ -211,6 +211,10 @@ int read_states(vmb_batch *b)
                                     cudaMemcpyDeviceToHost, b->stream);
     if (!e) e = cudaStreamSynchronize(b->stream);
     if (e) return cuda_fail(e, "batch states");
+    for (size_t k = 0; k < b->fits.size(); ++k)
+        if (b->fits[k].live && b->hostStates[k].errors)
+            return fail(VM_ERR_CUDA, "kernel error bits 0x" + std::to_string(b->hostStates[k].errors) + " in fit " +
+                                         std::to_string(k));
     return VM_OK;
 }
 

@@ -331,6 +331,14 @@ int ensure_graph(vm_optimizer *h)
     return VM_OK;
 }
 
+// Error bits a kernel raised in the fit's state (VM_KERR_*), as a status.
+int kernel_status(int bits)
+{
+    if (!bits) return VM_OK;
+    return fail(VM_ERR_CUDA, std::string("kernel error bits 0x") + std::to_string(bits) +
+                                 ((bits & VM_KERR_CAPACITY) ? " (deferred-target queue full)" : ""));
+}
+
 int read_state(vm_optimizer *h, VmState &st)
 {
     // through a pinned staging copy: one direct DMA per Step
@@ -724,7 +732,7 @@ int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
         if ((e = cudaGraphLaunch(h->graph, h->stream))) return cuda_fail(e, "graph launch");
     if ((e = cudaEventRecord(h->ev1, h->stream))) return cuda_fail(e, "event");
     VmState st;
-    if ((rc = read_state(h, st))) return rc;
+    if ((rc = read_state(h, st)) || (rc = kernel_status(st.errors))) return rc;
     h->iteration = st.iter;
     h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
     h->exactTotal = st.slowTotal;
@@ -766,7 +774,7 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
             return cuda_fail(e, "timed step");
     }
     VmState st;
-    if ((rc = read_state(h, st))) return rc;
+    if ((rc = read_state(h, st)) || (rc = kernel_status(st.errors))) return rc;
     h->iteration = st.iter;
     h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
     h->exactTotal = st.slowTotal;
@@ -815,7 +823,7 @@ int vm_evaluate_loss(vm_optimizer *h, float *loss)
         (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream)))
         return cuda_fail(e, "evaluate loss");
     VmState st;
-    if ((rc = read_state(h, st))) return rc;
+    if ((rc = read_state(h, st)) || (rc = kernel_status(st.errors))) return rc;
     *loss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
     return VM_OK;
 }

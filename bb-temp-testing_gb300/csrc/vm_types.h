@@ -33,8 +33,7 @@ struct VmState {
 };
 
 enum : int {
-    VM_KERR_GRID = 1,     // a site or target cell index fell outside its grid
-    VM_KERR_CAPACITY = 2, // a kNN or polygon buffer was too small
+    VM_KERR_CAPACITY = 2, // the deferred-target queue was full (it holds every live target, so never in practice)
 };
 
 struct VmFit {
