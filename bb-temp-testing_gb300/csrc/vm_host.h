@@ -57,12 +57,10 @@ template <class T> struct DevBuf {
     int reserve(size_t count) { return count <= n && p ? VM_OK : alloc(count); }
 };
 
+// The host part of the last Extract: the boundary (vertices, edges) and the
+// summary; the cells themselves stay on the device until copied out.
 struct MeshHost {
-    std::vector<float2> generators;
-    std::vector<uint8_t> inside;
-    std::vector<int> cellStart;
-    std::vector<float2> cellVerts;
-    std::vector<int> cellLabels;
+    int numGenerators = 0, numCellVerts = 0;
     std::vector<float2> vertices;
     std::vector<int> edges; // pairs
     bool watertight = false;

@@ -118,6 +118,8 @@ struct vm_optimizer {
     DevBuf<unsigned long long> bndKeys;
     DevBuf<unsigned> bndSlot;
     DevBuf<float2> bndPt, bndVerts;
+    DevBuf<float2> meshGen;          // the last Extract's generators
+    DevBuf<unsigned char> meshInside; // and occupancy flags
     DevBuf<float2> csrVerts;
     DevBuf<int> dPre; // [0, siteBlocks, 0, tiles, 0, lossTiles, 0, targetBlocks]
     DevBuf<int> dTPre; // [0, targetBlocks, 0, targetKeyTiles]
@@ -1061,19 +1063,17 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
             (e = cudaStreamSynchronize(h->stream)))
             return cuda_fail(e, "boundary assembly");
     }
+    // the cells stay on the device until vm_mesh_copy copies them straight
+    // into the caller's arrays (one copy); the generators and occupancy
+    // flags are snapshotted, since a Step or SetGenerators changes them
     MeshHost &M = h->mesh;
-    M.generators.resize(n);
-    M.inside.resize(n);
-    M.cellStart.resize((size_t)n + 1);
-    M.cellVerts.resize((size_t)total);
-    M.cellLabels.resize((size_t)total);
-    if ((e = cudaMemcpyAsync(M.cellStart.data(), h->cellStartD.p, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, h->stream)) ||
-        (total && (e = cudaMemcpyAsync(M.cellVerts.data(), h->csrVerts.p, sizeof(float2) * (size_t)total, cudaMemcpyDeviceToHost, h->stream))) ||
-        (total && (e = cudaMemcpyAsync(M.cellLabels.data(), h->csrLabels.p, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, h->stream))) ||
-        (e = cudaMemcpyAsync(M.inside.data(), h->inside.p, n, cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(M.generators.data(), h->gen.p, sizeof(float2) * n, cudaMemcpyDeviceToHost, h->stream)) ||
+    if ((rc = h->meshGen.reserve(n)) || (rc = h->meshInside.reserve(n))) return rc;
+    if ((e = cudaMemcpyAsync(h->meshGen.p, h->gen.p, sizeof(float2) * n, cudaMemcpyDeviceToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->meshInside.p, h->inside.p, n, cudaMemcpyDeviceToDevice, h->stream)) ||
         (e = cudaMemcpyAsync(flags, h->flags.p, sizeof(flags), cudaMemcpyDeviceToHost, h->stream)))
         return cuda_fail(e, "extract read");
+    M.numGenerators = n;
+    M.numCellVerts = total;
     M.edges.resize((size_t)occ);
     M.vertices.resize((size_t)nVert);
     int bndErr = 0;
@@ -1090,7 +1090,7 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
     boundary_topology(M);
     M.hostMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     info->numGenerators = n;
-    info->numCellVerts = (int)M.cellVerts.size();
+    info->numCellVerts = total;
     info->numVertices = (int)M.vertices.size();
     info->numEdges = (int)(M.edges.size() / 2);
     info->watertight = M.watertight ? 1 : 0;
@@ -1105,16 +1105,27 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
 int vm_mesh_copy(vm_optimizer *h, float *generators, uint8_t *inside, int *cellStart, float *cellVerts, float *vertices,
                  int *edges, int *cellLabels)
 {
+    vmh::NvtxRange range("vm_mesh_copy");
     if (!h) return fail(VM_ERR_ARG, "NULL handle");
     const MeshHost &M = h->mesh;
-    if (generators) std::memcpy(generators, M.generators.data(), sizeof(float2) * M.generators.size());
-    if (inside) std::memcpy(inside, M.inside.data(), M.inside.size());
-    if (cellStart) std::memcpy(cellStart, M.cellStart.data(), sizeof(int) * M.cellStart.size());
-    if (cellVerts) std::memcpy(cellVerts, M.cellVerts.data(), sizeof(float2) * M.cellVerts.size());
+    const size_t n = (size_t)M.numGenerators, total = (size_t)M.numCellVerts;
+    cudaError_t e = cudaSuccess;
+    if (n) {
+        if (!e && generators) e = cudaMemcpyAsync(generators, h->meshGen.p, sizeof(float2) * n, cudaMemcpyDeviceToHost, h->stream);
+        if (!e && inside) e = cudaMemcpyAsync(inside, h->meshInside.p, n, cudaMemcpyDeviceToHost, h->stream);
+        if (!e && cellStart)
+            e = cudaMemcpyAsync(cellStart, h->cellStartD.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (total) {
+        if (!e && cellVerts)
+            e = cudaMemcpyAsync(cellVerts, h->csrVerts.p, sizeof(float2) * total, cudaMemcpyDeviceToHost, h->stream);
+        if (!e && cellLabels)
+            e = cudaMemcpyAsync(cellLabels, h->csrLabels.p, sizeof(int) * total, cudaMemcpyDeviceToHost, h->stream);
+    }
     if (vertices) std::memcpy(vertices, M.vertices.data(), sizeof(float2) * M.vertices.size());
     if (edges) std::memcpy(edges, M.edges.data(), sizeof(int) * M.edges.size());
-    if (cellLabels) std::memcpy(cellLabels, M.cellLabels.data(), sizeof(int) * M.cellLabels.size());
-    return VM_OK;
+    if (!e) e = cudaStreamSynchronize(h->stream);
+    return e ? cuda_fail(e, "vm_mesh_copy") : VM_OK;
 }
 
 // ===========================================================================

@@ -284,9 +284,10 @@ def run_batch(args):
 
 
 def run_extract(args):
-    """Mesh extraction: the Voronoi-cell clipper (GPU) and the CSR packing,
-    boundary assembly (both on the GPU) and copy-out to the host
-    (host_assembly_ms) on the 1M-site fit after 50 steps, and on the
+    """Mesh extraction: the Voronoi-cell clipper (GPU), the CSR packing and
+    boundary assembly (both on the GPU, host_assembly_ms with the boundary
+    read-back) and the whole Extract() call with the mesh copied into numpy
+    arrays (extract_wall_ms), on the 1M-site fit after 50 steps, and on the
     512x512 lattice with 1e-6 jitter (near-cocircular bisectors); occupancy is
     a disc of radius 0.6 at the domain centre on a half-spacing voxel grid.
     cells/s = sites / clipper GPU time."""
@@ -317,12 +318,17 @@ def run_extract(args):
         if steps:
             o.Step(steps)
         o.Extract()  # warm-up
-        runs = [o.Extract() for _ in range(3)]
+        runs, walls = [], []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            runs.append(o.Extract())
+            walls.append((time.perf_counter() - t0) * 1e3)
         o.close()
         m = min(runs, key=lambda r: r.gpuMs)
         n = int((m.generators[:, 0] >= 0).sum())
         return {"sites": n, "steps_before": steps, "clipper_gpu_ms": m.gpuMs, "cells_per_s": n / (m.gpuMs / 1e3),
-                "host_assembly_ms": min(r.hostMs for r in runs), "watertight": bool(m.watertight), "loops": m.loops,
+                "host_assembly_ms": min(r.hostMs for r in runs), "extract_wall_ms": min(walls),
+                "watertight": bool(m.watertight), "loops": m.loops,
                 "unsafe_cells": m.unsafeCells, "overflow_cells": m.overflowCells,
                 "cell_verts": int(len(m.cellVerts)), "edges": int(len(m.edges))}
 
