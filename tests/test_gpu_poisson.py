@@ -51,3 +51,16 @@ def test_resample_many_equals_one_by_one(vm, orc):
     with pytest.raises(vm.VmError):
         s = vm.Sampler(1.0, 1.0, 0.02)
         vm.resample_many([s, s], [(0, 0, 4, 4), (4, 4, 8, 8)])
+
+
+def test_tiled_rounds_many_tiles(vm, orc):
+    """A fill and a region resample large enough for the tiled
+    one-launch-per-round path, spanning many 64-cell tiles in both directions,
+    with a region origin off the tile and colour grids."""
+    s = vm.Sampler(3.0, 2.0, 0.004, 30, 11)
+    region = (37, 53, 900, 650)
+    s.Resample(*region)
+    assert s.Verify(*region)
+    cells, _ = orc.poisson_fill(3.0, 2.0, 0.004, 30, 11, [region])
+    assert np.array_equal(s.Cells(), cells)
+    assert s.VerifyAll()
