@@ -109,6 +109,7 @@ int fail_budget(const char *what) { return fail(VM_ERR_BUDGET, what); }
 struct vmb_batch {
     Arena arena;
     cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr; // one step of the current fit set (captured after each table rebuild)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int maxFits = 0;
     std::vector<BFit> fits;          // by fit id
@@ -185,6 +186,8 @@ int rebuild_tables(vmb_batch *b)
         (e = cudaStreamSynchronize(b->stream)))
         return cuda_fail(e, "batch tables");
     b->dirty = false;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
     return VM_OK;
 }
 
@@ -201,6 +204,23 @@ int enqueue_batch_step(vmb_batch *b)
         (e = vm_launch_scatter(b->dSites.p, sitePre, nf, b->siteBlocks, b->dFits.p, b->stream)))
         return cuda_fail(e, "batch step");
     return VM_OK;
+}
+
+// The step of the current fit set as a CUDA graph (captured once per table
+// rebuild, replayed every step).
+int ensure_batch_graph(vmb_batch *b)
+{
+    if (b->graph) return VM_OK;
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e) return cuda_fail(e, "batch capture");
+    int rc = enqueue_batch_step(b);
+    e = cudaStreamEndCapture(b->stream, &g);
+    if (rc) return rc;
+    if (e) return cuda_fail(e, "batch capture");
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    return e ? cuda_fail(e, "batch graph") : VM_OK;
 }
 
 int read_states(vmb_batch *b)
@@ -266,6 +286,7 @@ int vmb_destroy(vmb_batch *b)
 {
     if (!b) return VM_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -485,10 +506,11 @@ int vmb_step(vmb_batch *b, int iterations, float *gpuMs)
     int rc;
     if (b->dirty && (rc = rebuild_tables(b))) return rc;
     if (b->order.empty() || iterations == 0) return VM_OK;
+    if ((rc = ensure_batch_graph(b))) return rc;
     cudaError_t e;
     if ((e = cudaEventRecord(b->ev0, b->stream))) return cuda_fail(e, "event");
     for (int k = 0; k < iterations; ++k)
-        if ((rc = enqueue_batch_step(b))) return rc;
+        if ((e = cudaGraphLaunch(b->graph, b->stream))) return cuda_fail(e, "batch graph launch");
     if ((e = cudaEventRecord(b->ev1, b->stream)) || (e = cudaEventSynchronize(b->ev1))) return cuda_fail(e, "event");
     float ms = 0;
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
