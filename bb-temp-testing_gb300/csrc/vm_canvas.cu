@@ -49,6 +49,7 @@ constexpr int kMaxVoxelsX = 131072;
 constexpr int kBigBlocks = 32;
 constexpr int kListBlocks = 1024; // blocks of the tile work-list kernels (8 warps each)
 constexpr int kMaxBucketEntries = 1 << 27; // beyond this the scanline kernels test every edge
+constexpr int kMaxRimSamples = 1 << 28;    // rim samples of one stamp (radius / voxel size < 10.6M)
 
 enum { kErrSamples = 1, kErrCrossings = 2, kErrRimBox = 4 };
 
@@ -1205,8 +1206,15 @@ int cv_rasterize(cv_canvas *c, const float *xy, int n, float *gpuMs)
     }
     if ((e = cudaEventRecord(c->ev1, s))) return cuda_fail(e, "event");
     if ((rc = read_state(c))) return rc;
-    if (c->st.err & kErrCrossings)
+    if (c->st.err & kErrCrossings) {
+        // leave the canvas empty, as a rasterisation of no polygon does
+        if ((e = cudaMemsetAsync(c->dState.p, 0, sizeof(CvState), s)) ||
+            (e = cudaMemsetAsync(c->inside.p, 0, c->tiles * 8, s)) ||
+            (e = cudaMemsetAsync(c->smask.p, 0, c->tiles * 8, s)))
+            return cuda_fail(e, "cv_rasterize reset");
+        if ((rc = read_state(c))) return rc;
         return fail(VM_ERR_UNSUPPORTED, "cv_rasterize: more than 32768 polygon edges cross one scanline");
+    }
     if (gpuMs && (e = cudaEventElapsedTime(gpuMs, c->ev0, c->ev1))) return cuda_fail(e, "event time");
     return VM_OK;
 }
@@ -1217,18 +1225,29 @@ int cv_stamp_disc(cv_canvas *c, float cx, float cy, float radius, int inside, cv
     if (!c || !out) return fail(VM_ERR_ARG, "cv_stamp_disc: bad arguments");
     *out = cv_edit{};
     c->lastEdit = cv_edit{};
+    if (!std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(radius))
+        return fail(VM_ERR_ARG, "cv_stamp_disc: centre and radius must be finite");
     const CvGeom g = c->g;
     cudaStream_t s = c->stream;
-    // canvas.cpp:138-146, the same float operations as the reference
+    // canvas.cpp:138-146, the same float operations as the reference; the
+    // voxel indices are clamped before the conversion to int (lower bounds to
+    // [0, size], upper to [-1, size - 1]), which keeps i0 > i1 exactly when
+    // the reference's box is empty
     const float inv = 1.0f / g.vs;
     const float r2 = radius * radius;
-    int i0 = std::max((int)std::floor((cx - radius) * inv), 0);
-    int j0 = std::max((int)std::floor((cy - radius) * inv), 0);
-    int i1 = std::min((int)std::floor((cx + radius) * inv), g.vx - 1);
-    int j1 = std::min((int)std::floor((cy + radius) * inv), g.vy - 1);
+    auto index = [](float v, int lo, int hi) {
+        float f = std::floor(v);
+        return f < (float)lo ? lo : f > (float)hi ? hi : (int)f;
+    };
+    int i0 = index((cx - radius) * inv, 0, g.vx);
+    int j0 = index((cy - radius) * inv, 0, g.vy);
+    int i1 = index((cx + radius) * inv, -1, g.vx - 1);
+    int j1 = index((cy + radius) * inv, -1, g.vy - 1);
     if (i0 > i1 || j0 > j1) return VM_OK;
     // rim sample positions: the reference's host trigonometry (canvas.cpp:151-154)
-    int n = std::max(16, (int)std::ceil(2.0f * 3.14159265f * radius / (0.25f * g.vs)));
+    const float rimF = std::ceil(2.0f * 3.14159265f * radius / (0.25f * g.vs));
+    if (!(rimF <= (float)kMaxRimSamples)) return fail(VM_ERR_UNSUPPORTED, "cv_stamp_disc: radius too large");
+    int n = std::max(16, (int)rimF);
     c->rimHost.resize((size_t)n);
     for (int k = 0; k < n; ++k) {
         float a = 2.0f * 3.14159265f * (float)k / (float)n;

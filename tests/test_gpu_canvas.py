@@ -69,14 +69,17 @@ def test_rasterize_without_edge_buckets(vm, orc, monkeypatch, name):
 
 def test_rasterize_crossing_limit(vm, orc):
     """A scanline crossed by more than 32768 edges is reported as unsupported
-    (status 7) without touching the device state beyond this call; one just
-    under the limit (block-per-row path) still matches the oracle."""
+    (status 7) and leaves the canvas empty; one just under the limit
+    (block-per-row path) still matches the oracle."""
     from voromesh_gb300 import synth
 
     c = vm.Canvas(131072.0, 16.0, 1.0)
+    c.RasterizeShape(synth.heart(64.0, 8.0, 12.0, 64))
+    assert c.SurfaceCount() > 0
     with pytest.raises(vm.VmError) as err:
         c.RasterizeShape(synth.comb(1.0, 2.0, 131000.0, 10.0, 17000))
     assert err.value.code == 7
+    assert c.SurfaceCount() == 0 and c.TargetSlots().shape == (0, 2) and not c.InsideMasks().any()
     c.close()
     poly = synth.comb(1.0, 2.0, 60000.0, 10.0, 8000)  # 16000 crossings
     c = vm.Canvas(65536.0, 16.0, 1.0)
@@ -151,6 +154,31 @@ def test_stamp_edges(vm, orc):
     poly = synth.heart(30.0, 20.0, 30.0, 64)
     c.RasterizeShape(poly)
     o.rasterize(poly)
+    _same(c.state(), o.state(), orc)
+
+
+def test_stamp_rejects_bad_input(vm, orc):
+    """A non-finite centre or radius is an argument error and a radius whose
+    rim needs more than 2^28 samples is unsupported; neither changes the
+    canvas. Centres far off the domain (beyond the int range in voxels) are
+    empty edits."""
+    from voromesh_gb300 import synth
+
+    poly = synth.heart(32.0, 32.0, 50.0, 300)
+    c = vm.Canvas(64.0, 64.0, 1.0)
+    o = orc.Canvas(64.0, 64.0, 1.0)
+    c.RasterizeShape(poly)
+    o.rasterize(poly)
+    for cx, cy, r in [(np.nan, 3.0, 2.0), (3.0, np.inf, 2.0), (3.0, 3.0, np.nan)]:
+        with pytest.raises(vm.VmError) as err:
+            c.StampDisc((cx, cy), r, True)
+        assert err.value.code == 1
+    with pytest.raises(vm.VmError) as err:
+        c.StampDisc((32.0, 32.0), 1e9, False)
+    assert err.value.code == 7
+    for cx, cy in [(3e10, 5.0), (-3e10, 5.0), (5.0, 3e10), (5.0, -3e10)]:
+        e = c.StampDisc((cx, cy), 4.0, True)
+        assert not e.Changed() and len(e.dirtySlots) == 0
     _same(c.state(), o.state(), orc)
 
 
