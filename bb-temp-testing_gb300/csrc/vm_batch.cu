@@ -665,7 +665,7 @@ int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result 
             }
             continue;
         }
-        // step all live fits together, then judge each on its full-target loss:
+        // step all live fits together, then test each against its full-target loss:
         // the loss pass of the round's last step when every target counts every
         // step (sampleFraction 1), else a separate full-target evaluation
         bool evaluate = false;
