@@ -43,6 +43,7 @@ N_SITES = 1048576
 N_TARGETS = 8388608
 K = 16
 RADIUS = 1e-3
+METRIC = "site-steps/s @1M sites k=16"
 LR_PER_SPACING = 0.09
 KERNELS_PER_STEP = 6  # k_loss, k_loss_exact, k_adam_bin, k_scan_tiles, k_scan_apply, k_scatter
 
@@ -222,7 +223,7 @@ def run_reference(args, world, rank):
     dt = time.perf_counter() - t0
     v = len(g) * args.steps / dt
     line = {
-        "impl": "reference", "metric": "site-steps/s @1M sites k=16", "value": v, "unit": "site-steps/s",
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "site-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "scale_1m: 1,048,576 generators (Poisson r=1e-3 subset), 8,388,608 targets on a "
@@ -666,7 +667,7 @@ def main():
 
     if rank == 0:
         line = {
-            "metric": "site-steps/s @1M sites k=16", "value": value, "unit": "site-steps/s", "n_gpus": world,
+            "metric": METRIC, "value": value, "unit": "site-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
