@@ -64,6 +64,7 @@ def lib() -> C.CDLL:
         _lib.vo_fit64_eval_loss.argtypes = [C.c_void_p]
         _lib.vo_fit64_get.argtypes = [C.c_void_p, C.c_void_p]
         _lib.vo_fit64_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.vo_fit64_detail.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.vo_poisson_resample.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.vo_poisson_verify.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.vo_poisson_init.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_int, C.c_uint]
@@ -291,6 +292,7 @@ class Fit64:
         self.h = C.c_void_p(lib().vo_fit64_create(width, height, spacing, K, lrPerSpacing, sampleFraction, gamma, ms,
                                                   params_iterations, seed, nthreads))
         self.n = 0
+        self.nt = 1
 
     def __del__(self):
         try:
@@ -300,6 +302,7 @@ class Fit64:
 
     def set_targets(self, t):
         t = np.ascontiguousarray(t, np.float32)
+        self.nt = max(len(t), 1)
         lib().vo_fit64_set_targets(self.h, P(t), len(t))
 
     def set_generators(self, g, slotsW, slotsH, slotCellSize):
@@ -324,6 +327,14 @@ class Fit64:
         loss = C.c_double()
         lib().vo_fit64_gradient(self.h, P(g), C.byref(cnt), C.byref(loss))
         return g, cnt.value, loss.value
+
+    def detail(self):
+        """Per target (nearest site, bisector neighbour) of the full-target
+        pass at the current generators, in double (-1 = unused)."""
+        i0 = np.empty(self.nt, np.int32)
+        j = np.empty(self.nt, np.int32)
+        lib().vo_fit64_detail(self.h, P(i0), P(j))
+        return i0, j
 
 
 def poisson_fill(width, height, radius, trials=30, seed=1, regions=()):

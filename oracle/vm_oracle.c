@@ -940,6 +940,7 @@ typedef struct {
     double loss[256];
     int count[256];
     pthread_mutex_t *mu;
+    int *i0Out, *jOut; /* optional per-target decisions (-1 = unused) */
 } vo_l64_job;
 
 static void loss64_range(void *ctx, int64_t lo, int64_t hi, int tid)
@@ -952,6 +953,7 @@ static void loss64_range(void *ctx, int64_t lo, int64_t hi, int tid)
     double d2[64];
     for (int64_t ii = lo; ii < hi; ++ii) {
         int i = (int)ii;
+        if (J->i0Out) J->i0Out[i] = J->jOut[i] = -1;
         double px = f->targets[2 * i], py = f->targets[2 * i + 1];
         int take = px >= 0.0;
         if (take && J->useBox) take = px >= f->bx0 && px <= f->bx1 && py >= f->by0 && py <= f->by1;
@@ -973,6 +975,10 @@ static void loss64_range(void *ctx, int64_t lo, int64_t hi, int tid)
             if (d * d < best) { best = d * d; bestD = d; bestJ = j; }
         }
         if (bestJ < 0) continue;
+        if (J->i0Out) {
+            J->i0Out[i] = i0;
+            J->jOut[i] = bestJ;
+        }
         loss += best;
         ++cnt;
         if (J->wantGrad) {
@@ -993,9 +999,12 @@ static void loss64_range(void *ctx, int64_t lo, int64_t hi, int tid)
     J->count[tid] = cnt;
 }
 
-static void loss64(vo_fit64 *f, int useBox, double fraction, unsigned iter, int wantGrad, double *loss, int *count)
+static void loss64_detail(vo_fit64 *f, int useBox, double fraction, unsigned iter, int wantGrad, double *loss,
+                          int *count, int *i0Out, int *jOut)
 {
     vo_l64_job *J = (vo_l64_job *)calloc(1, sizeof(vo_l64_job));
+    J->i0Out = i0Out;
+    J->jOut = jOut;
     pthread_mutex_t mu = PTHREAD_MUTEX_INITIALIZER;
     J->f = f;
     J->useBox = useBox;
@@ -1010,6 +1019,11 @@ static void loss64(vo_fit64 *f, int useBox, double fraction, unsigned iter, int 
     *loss = l;
     *count = c;
     free(J);
+}
+
+static void loss64(vo_fit64 *f, int useBox, double fraction, unsigned iter, int wantGrad, double *loss, int *count)
+{
+    loss64_detail(f, useBox, fraction, iter, wantGrad, loss, count, NULL, NULL);
 }
 
 double vo_fit64_step(vo_fit64 *f, int steps)
@@ -1064,6 +1078,16 @@ double vo_fit64_eval_loss(vo_fit64 *f)
 void vo_fit64_get(const vo_fit64 *f, double *gen)
 {
     memcpy(gen, f->gen, sizeof(double) * 2 * (size_t)f->slotsW * f->slotsH);
+}
+
+/* Per target: nearest site and bisector neighbour of the full-target pass
+ * (EvaluateLoss's decisions) at the current generators, in double. */
+void vo_fit64_detail(vo_fit64 *f, int *i0, int *j)
+{
+    double loss;
+    int count;
+    grid64(f);
+    loss64_detail(f, 0, 1.0, (unsigned)f->iter, 0, &loss, &count, i0, j);
 }
 
 void vo_fit64_gradient(vo_fit64 *f, double *grad, int *count, double *loss)

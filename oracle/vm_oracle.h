@@ -144,6 +144,7 @@ double vo_fit64_step(vo_fit64 *f, int steps);
 double vo_fit64_eval_loss(vo_fit64 *f);
 void vo_fit64_get(const vo_fit64 *f, double *gen);
 void vo_fit64_gradient(vo_fit64 *f, double *grad, int *count, double *loss);
+void vo_fit64_detail(vo_fit64 *f, int *i0, int *j);
 
 /* ---- extraction ------------------------------------------------------------------
  * voronoiCellKernel (voro_optimizer.cu:361-437): FP64 Sutherland-Hodgman

@@ -135,6 +135,34 @@ def test_fp64_error_bar(orc, plain):
     assert err < 1e-3  # a few lr; bisector flips between FP32 and FP64 are discrete
 
 
+@pytest.mark.parametrize("shape", ["plain", "lattice_jitter", "lattice_exact"])
+def test_decisions_equal_fp64(orc, plain, shape):
+    """At the same generator positions, every target's nearest site and
+    bisector neighbour in FP32 (the product's, which equals this oracle bit
+    for bit) are those of the FP64 oracle: no decision flips, along the FP32
+    trajectory. Later FP32/FP64 position differences come from the
+    trajectories parting, not from the decisions' arithmetic."""
+    from voromesh_gb300 import synth
+
+    if shape == "plain":
+        gen, sw, sh, tgt, spacing, K = plain.generators, 2048, 1, plain.targets, 0.05, 12
+    else:
+        gen = synth.lattice(3, 5, 128, 128, 1e-6 if shape == "lattice_jitter" else 0.0)
+        sw, sh, tgt, spacing, K = 128, 128, synth.five_arm_star(3, 6, 131072), 2.0 / 128, 16
+    f = orc.Fit(2.0, 2.0, spacing, K, 0.09, 1.0, 300, nthreads=4)
+    f.set_targets(tgt)
+    f.set_generators(gen, sw, sh, 2.0)
+    for steps in (0, 10):
+        f.step(steps)
+        d = orc.Fit64(2.0, 2.0, float(np.float32(spacing)), K, 0.09, 1.0, 300, nthreads=4)
+        d.set_targets(tgt)
+        d.set_generators(f.generators()[0], sw, sh, 2.0)
+        i0, j, _ = orc.loss_detail(f, tgt, K)
+        i64, j64 = d.detail()
+        assert (i0 >= 0).sum() > 0.99 * len(tgt)
+        assert np.array_equal(i0, i64) and np.array_equal(j, j64)
+
+
 def test_cells(orc, gold):
     from voromesh_gb300 import synth
 
