@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit", "poisson", "canvas"],
                     help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads; "
-                         "extract: the cell clipper; edit: the local-edit pipeline; poisson: the sampler")
+                         "extract: the cell clipper; edit: the local-edit pipeline; poisson: the sampler; "
+                         "canvas: RasterizeShape and StampDisc")
     ap.add_argument("--fits", type=int, default=512)
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--requests", type=int, default=200)
