@@ -54,9 +54,8 @@ def test_resample_many_equals_one_by_one(vm, orc):
 
 
 def test_tiled_rounds_many_tiles(vm, orc):
-    """A fill and a region resample large enough for the tiled
-    one-launch-per-round path, spanning many 64-cell tiles in both directions,
-    with a region origin off the tile and colour grids."""
+    """A region resample over half a million cells whose origin is off the colour grid,
+    then the whole-grid check."""
     s = vm.Sampler(3.0, 2.0, 0.004, 30, 11)
     region = (37, 53, 900, 650)
     s.Resample(*region)
@@ -64,3 +63,19 @@ def test_tiled_rounds_many_tiles(vm, orc):
     cells, _ = orc.poisson_fill(3.0, 2.0, 0.004, 30, 11, [region])
     assert np.array_equal(s.Cells(), cells)
     assert s.VerifyAll()
+
+
+def test_regions_with_outside_neighbours_and_many_rounds(vm, orc):
+    """Large regions whose conflict neighbourhoods reach outside them (samples
+    kept from earlier calls), a whole-grid region among them, and a sampler
+    with 260 rounds per call: the oracle's samples."""
+    s = vm.Sampler(2.0, 1.0, 0.013, 30, 5)
+    regions = [(10, 10, 200, 100), (0, 0, 218, 109), (-5, 30, 120, 200), (57, 3, 190, 71)]
+    for reg in regions:
+        s.Resample(*reg)
+        assert s.Verify(*reg)
+    cells, _ = orc.poisson_fill(2.0, 1.0, 0.013, 30, 5, regions)
+    assert np.array_equal(s.Cells(), cells)
+    s = vm.Sampler(1.0, 1.0, 0.02, 260, 2)
+    cells, _ = orc.poisson_fill(1.0, 1.0, 0.02, 260, 2)
+    assert np.array_equal(s.Cells(), cells)
