@@ -216,8 +216,11 @@ int ensure_batch_graph(vmb_batch *b)
     if (e) return cuda_fail(e, "batch capture");
     int rc = enqueue_batch_step(b);
     e = cudaStreamEndCapture(b->stream, &g);
-    if (rc) return rc;
-    if (e) return cuda_fail(e, "batch capture");
+    if (e) return rc ? rc : cuda_fail(e, "batch capture");
+    if (rc) {
+        cudaGraphDestroy(g);
+        return rc;
+    }
     e = cudaGraphInstantiate(&b->graph, g, 0);
     cudaGraphDestroy(g);
     return e ? cuda_fail(e, "batch graph") : VM_OK;

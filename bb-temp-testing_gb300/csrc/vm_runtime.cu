@@ -325,8 +325,11 @@ int ensure_graph(vm_optimizer *h)
     if (e) return cuda_fail(e, "begin capture");
     int rc = enqueue_step(h);
     e = cudaStreamEndCapture(h->stream, &g);
-    if (rc) return rc;
-    if (e) return cuda_fail(e, "end capture");
+    if (e) return rc ? rc : cuda_fail(e, "end capture");
+    if (rc) {
+        cudaGraphDestroy(g);
+        return rc;
+    }
     e = cudaGraphInstantiate(&h->graph, g, 0);
     cudaGraphDestroy(g);
     if (e) return cuda_fail(e, "graph instantiate");

@@ -199,7 +199,9 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *fit, int *fitId);
 int vmb_remove_fit(vmb_batch *b, int fitId);
 /* Inactive fits keep their memory but are not stepped. */
 int vmb_set_active(vmb_batch *b, int fitId, int active);
-/* `iterations` steps of every active fit; GPU ms of the whole run. */
+/* `iterations` steps of every active fit; GPU ms of the whole run. It reads
+ * nothing back: a fit's kernel error bits surface as VM_ERR_CUDA at the next
+ * vmb_evaluate or vmb_fit_info. */
 int vmb_step(vmb_batch *b, int iterations, float *gpuMs);
 /* EvaluateLoss() of every active fit; losses[fitId] (maxFits entries). */
 int vmb_evaluate(vmb_batch *b, float *losses);
