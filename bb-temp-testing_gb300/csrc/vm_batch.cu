@@ -313,10 +313,17 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     vmh::NvtxRange range("vmb_add_fit");
     if (!b || !in || !fitId) return fail(VM_ERR_ARG, "vmb_add_fit: bad arguments");
     *fitId = -1;
-    int n = in->slotsW * in->slotsH;
-    if (in->slotsW < 0 || in->slotsH < 0 || n < 0 || in->nTargets < 0 || (n > 0 && !in->generators) ||
-        (in->nTargets > 0 && !in->targets) || !(in->width > 0) || !(in->height > 0) || !(in->spacing > 0))
+    if (in->slotsW < 0 || in->slotsH < 0 || in->nTargets < 0 || !(in->width > 0) || !(in->height > 0) ||
+        !(in->spacing > 0))
         return fail(VM_ERR_ARG, "vmb_add_fit: bad fit");
+    // the single-fit limits: slots as in vm_set_generators, the hash grid as in vm_create
+    const long long n64 = (long long)in->slotsW * in->slotsH;
+    if (n64 > 0x7FFFFFFF / kMaxCellVerts) return fail(VM_ERR_ARG, "vmb_add_fit: too many generator slots");
+    if ((double)std::ceil(in->width / in->spacing) * (double)std::ceil(in->height / in->spacing) > 1.5e9)
+        return fail(VM_ERR_ARG, "vmb_add_fit: hash grid too large");
+    const int n = (int)n64;
+    if ((n > 0 && !in->generators) || (in->nTargets > 0 && !in->targets))
+        return fail(VM_ERR_ARG, "vmb_add_fit: NULL buffer");
     int K = in->params.lossK;
     if (K != 8 && K != 12 && K != 16 && K != 24 && K != 32) return fail(VM_ERR_UNSUPPORTED, "lossK");
     int id = -1;
