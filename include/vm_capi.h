@@ -22,6 +22,7 @@
 #ifndef VM_CAPI_H
 #define VM_CAPI_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus

@@ -21,7 +21,7 @@ def libpath():
 def _declared_c_functions():
     text = (ROOT / "include" / "vm_capi.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:vm|pd|cv)_\w+)\s*\(", text, flags=re.M)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:vm|vmb|vms|pd|cv)_\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
@@ -39,6 +39,8 @@ def test_every_c_function_is_exported(libpath):
     lib = ctypes.CDLL(str(libpath))
     names = _declared_c_functions()
     assert len(names) >= 30
+    for prefix in ("vm_", "vmb_", "vms_", "pd_", "cv_"):
+        assert any(n.startswith(prefix) for n in names), prefix
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 
@@ -69,3 +71,34 @@ def test_status_codes_without_gpu(libpath):
     assert lib.cv_create(C.c_float(1.0), C.c_float(1.0), C.c_float(0.0), C.byref(C.c_void_p())) == 1
     buf = C.create_string_buffer(256)
     assert lib.vm_last_error(buf, 256) == 0 and len(buf.value) > 0
+
+
+C_CALLER = r"""
+#include "vm_capi.h"
+#include <stdio.h>
+int main(void)
+{
+    int major = 0, minor = 0, sm = 0;
+    char msg[256];
+    vm_optimizer *h = NULL;
+    int rv = vm_version(&major, &minor, &sm);
+    int rc = vm_create(-1.0f, 1.0f, 1.0f, NULL, &h);
+    vm_last_error(msg, (int)sizeof msg);
+    printf("%d %d %d %d\n", rv, major, rc, h == NULL);
+    return 0;
+}
+"""
+
+
+def test_c_header_is_plain_c(libpath, tmp_path):
+    """include/vm_capi.h compiles as C99 on its own (what a cgo or C binding
+    includes) and a C caller links and runs against the library."""
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", f"-I{ROOT / 'include'}",
+                        str(src), f"-L{libpath.parent}", "-lvoromesh_gb300", f"-Wl,-rpath,{libpath.parent}", "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout.split() == ["0", "1", "1", "1"], out.stdout + out.stderr
