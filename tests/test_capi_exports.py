@@ -102,3 +102,14 @@ def test_c_header_is_plain_c(libpath, tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0 and out.stdout.split() == ["0", "1", "1", "1"], out.stdout + out.stderr
+
+
+@pytest.mark.parametrize("header", ["voromesh/voro_optimizer.h", "voromesh/canvas.h", "voromesh/gb300_ext.h",
+                                    "voromesh/shape2d.h", "poisson/poisson_disk.h", "vm_capi.h"])
+def test_header_self_contained(header, tmp_path):
+    """Each public header compiles on its own as C++17."""
+    src = tmp_path / "h.cpp"
+    src.write_text(f'#include "{header}"\n')
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only",
+                        f"-I{ROOT / 'include'}", str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
