@@ -60,8 +60,9 @@ struct PdParams {
     int gridW, gridH;
     unsigned seed;
 };
+// dependentLaunch: each phase launch a programmatic dependent of the one before
 cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int trials,
-                               unsigned roundBase, cudaStream_t s);
+                               unsigned roundBase, cudaStream_t s, bool dependentLaunch);
 // One sampler's region resample for pd_launch_resample_many.
 struct PdJob {
     float2 *grid;

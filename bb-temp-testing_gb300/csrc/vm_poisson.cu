@@ -72,9 +72,16 @@ __global__ void __launch_bounds__(256) k_clear(float2 *grid, int gridW, int x0, 
 
 // One phase (px, py) of one round, one thread per phase cell: x across the
 // threads of a block row, phase rows over blockIdx.y.
+//
+// Launched as a programmatic dependent of the previous phase: the hardware
+// wait below returns once that phase has completed and its writes are
+// visible, and the early trigger lets the next phase's launch overlap this
+// one's tail. Without the launch attribute both instructions are no-ops.
 __global__ void __launch_bounds__(256) k_phase(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int px,
                                                int py, unsigned keyX, unsigned keyY)
 {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     int tw = (x1 - x0 - px + 2) / 3, th = (y1 - y0 - py + 2) / 3;
     int tx = blockIdx.x * blockDim.x + threadIdx.x;
     if (tx >= tw) return;
@@ -127,7 +134,7 @@ __global__ void __launch_bounds__(kSmallBlock) k_resample_many(const PdJob *__re
 using namespace vmk;
 
 cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int trials,
-                               unsigned roundBase, cudaStream_t s)
+                               unsigned roundBase, cudaStream_t s, bool dependentLaunch)
 {
     int rw = x1 - x0, rh = y1 - y0;
     if (rw <= 0 || rh <= 0) return cudaSuccess;
@@ -141,11 +148,24 @@ cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1,
     if (cb > 65535) cb = 65535;
     k_clear<<<cb, 256, 0, s>>>(grid, p.gridW, x0, y0, x1, y1);
     dim3 pb((unsigned)((rw + 2) / 3 + 255) / 256, (unsigned)std::min((rh + 2) / 3, 65535));
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = pb;
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = dependentLaunch ? 1 : 0;
     for (int round = 0; round < trials; ++round) {
         unsigned r = roundBase + (unsigned)round;
         unsigned kx = round_key(r, p.seed, 0u), ky = round_key(r, p.seed, 1u);
         for (int py = 0; py < 3; ++py)
-            for (int px = 0; px < 3; ++px) k_phase<<<pb, 256, 0, s>>>(grid, p, x0, y0, x1, y1, px, py, kx, ky);
+            for (int px = 0; px < 3; ++px) {
+                cudaError_t e = cudaLaunchKernelEx(&cfg, k_phase, grid, p, x0, y0, x1, y1, px, py, kx, ky);
+                if (e) return e;
+            }
     }
     return cudaGetLastError();
 }

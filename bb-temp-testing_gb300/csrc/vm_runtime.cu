@@ -1324,9 +1324,12 @@ int pd_resample(pd_sampler *s, int cx0, int cy0, int cx1, int cy1, float *gpuMs)
     int x0 = std::max(cx0, 0), y0 = std::max(cy0, 0), x1 = std::min(cx1, s->gridW), y1 = std::min(cy1, s->gridH);
     if (x0 >= x1 || y0 >= y1) return VM_OK;
     PdParams p{s->width, s->height, s->radius, s->cellSize, s->gridW, s->gridH, s->seed};
+    // phases as programmatic dependent launches unless VM_PD_PDL=0 (same samples)
+    const char *env = std::getenv("VM_PD_PDL");
+    const bool pdl = !(env && std::atoi(env) == 0);
     cudaError_t e;
     if ((e = cudaEventRecord(s->ev0, s->stream)) ||
-        (e = pd_launch_resample(s->grid.p, p, x0, y0, x1, y1, s->trials, s->roundBase, s->stream)) ||
+        (e = pd_launch_resample(s->grid.p, p, x0, y0, x1, y1, s->trials, s->roundBase, s->stream, pdl)) ||
         (e = cudaEventRecord(s->ev1, s->stream)))
         return cuda_fail(e, "resample");
     s->roundBase += (unsigned)s->trials;

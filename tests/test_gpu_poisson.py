@@ -65,10 +65,13 @@ def test_tiled_rounds_many_tiles(vm, orc):
     assert s.VerifyAll()
 
 
-def test_regions_with_outside_neighbours_and_many_rounds(vm, orc):
+@pytest.mark.parametrize("pdl", ["1", "0"])
+def test_regions_with_outside_neighbours_and_many_rounds(vm, orc, monkeypatch, pdl):
     """Large regions whose conflict neighbourhoods reach outside them (samples
     kept from earlier calls), a whole-grid region among them, and a sampler
-    with 260 rounds per call: the oracle's samples."""
+    with 260 rounds per call: the oracle's samples, with the phases launched
+    as programmatic dependents of each other or (VM_PD_PDL=0) plainly."""
+    monkeypatch.setenv("VM_PD_PDL", pdl)
     s = vm.Sampler(2.0, 1.0, 0.013, 30, 5)
     regions = [(10, 10, 200, 100), (0, 0, 218, 109), (-5, 30, 120, 200), (57, 3, 190, 71)]
     for reg in regions:
