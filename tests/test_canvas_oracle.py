@@ -13,6 +13,8 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import canvas_shapes
+
 GOLDEN = Path(__file__).resolve().parent / "golden" / "reference_canvas.npz"
 
 
@@ -77,6 +79,33 @@ def test_oracle_matches_live_reference(orc):
             assert np.array_equal(pi[ea.dirty[:ea.removed]], eb.dirty[:eb.removed])
             pi = orc.canvas_relabelling(a.state(), b.state())
             assert sorted(pi[ea.dirty[ea.removed:]].tolist()) == sorted(eb.dirty[eb.removed:].tolist())
+
+
+@pytest.mark.parametrize("name", canvas_shapes.NAMES)
+def test_oracle_matches_live_reference_on_edge_shapes(orc, name):
+    """Every shape the GPU parity tests use (self-intersecting, clockwise,
+    600-crossing scanlines, mixed-magnitude coordinates in one voxel, a
+    sliver, a single vertex), rasterised and then stamped, against the
+    reference's own Canvas."""
+    if not orc.ref_canvas_available():
+        pytest.skip("the reference canvas is not compiled here")
+    (w, h, vs), poly = canvas_shapes.shape(name)
+    a, b = orc.Canvas(w, h, vs), orc.RefCanvas(w, h, vs)
+    a.rasterize(poly)
+    b.rasterize(poly)
+    pi = orc.canvas_relabelling(a.state(), b.state())
+    assert np.array_equal(pi, np.arange(len(pi)))
+    rng = np.random.default_rng(sum(map(ord, name)))
+    for _ in range(12):
+        cx = np.float32(rng.uniform(-0.1 * w, 1.1 * w))
+        cy = np.float32(rng.uniform(-0.1 * h, 1.1 * h))
+        r = np.float32(rng.uniform(0.5, 0.2 * min(w, h) / vs) * vs)
+        ins = bool(rng.integers(2))
+        ea, eb = a.stamp(cx, cy, r, ins), b.stamp(cx, cy, r, ins)
+        assert ea.rect() == eb.rect() and ea.counts() == eb.counts()
+        assert np.array_equal(pi[ea.dirty[:ea.removed]], eb.dirty[:eb.removed])
+        pi = orc.canvas_relabelling(a.state(), b.state())
+        assert sorted(pi[ea.dirty[ea.removed:]].tolist()) == sorted(eb.dirty[eb.removed:].tolist())
 
 
 def test_relabelling_check_catches_a_planted_error(orc):
