@@ -1,11 +1,13 @@
-"""The oracle against golden vectors of the reference's own kernels.
+"""The oracle against the reference's own kernels.
 
 tests/golden/reference_kernels.npz was produced by tests/golden/make_golden.py
-from the reference's kernel code compiled for the CPU (oracle/ref_shim). The
-oracle's reference mode (float sums in target order, powf) must reproduce
-every array bit for bit; its fixed-point mode (the product's arithmetic) must
-stay within the stated tolerances.
+from the reference's kernel code compiled for the CPU (oracle/ref_shim); where
+that build is present (oracle/_ref), the tie-heavy lattice shape is also
+checked against it live. The oracle's reference mode (float sums in target
+order, powf) must reproduce every array bit for bit; its fixed-point mode (the
+product's arithmetic) must stay within the stated tolerances.
 """
+import ctypes as C
 from pathlib import Path
 
 import numpy as np
@@ -161,6 +163,61 @@ def test_decisions_equal_fp64(orc, plain, shape):
         i64, j64 = d.detail()
         assert (i0 >= 0).sum() > 0.99 * len(tgt)
         assert np.array_equal(i0, i64) and np.array_equal(j, j64)
+
+
+def _make_golden_module():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", Path(__file__).resolve().parent / "golden" /
+                                                  "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.mark.parametrize("jitter", [1e-6, 0.0])
+def test_lattice_matches_live_reference(orc, jitter):
+    """The tie-heavy shape (a 128x128 lattice of sites, jittered by 1e-6 or
+    exact, 131,072 targets on the 5-arm star, k=16) against the reference's own
+    kernels compiled for the CPU: the grid, kNN lists, the first gradient and
+    10 steps of positions and moments, with the oracle in reference mode."""
+    if not orc.ref_available():
+        pytest.skip("the reference kernels are not compiled here")
+    from voromesh_gb300 import synth
+
+    mg = _make_golden_module()
+    ref = orc.ref()
+    gen = np.ascontiguousarray(synth.lattice(3, 5, 128, 128, jitter).reshape(-1, 2))
+    tgt = np.ascontiguousarray(synth.five_arm_star(3, 6, 131072))
+    spacing, K, n = float(np.float32(2.0 / 128)), 16, len(gen)
+    gw, gh = orc.grid_dims(2.0, 2.0, spacing)
+    rst, rsi, rsp, rgc = mg.ref_grid(ref, gen, gw, gh, spacing)
+    f = orc.Fit(2.0, 2.0, spacing, K, 0.09, 1.0, 300, acc=orc.ACC_REF, pow_mode=orc.POW_REF, nthreads=4)
+    f.set_targets(tgt)
+    f.set_generators(gen, n, 1, 2.0)
+    start, sidx, spos, gcell = f.grid()
+    assert np.array_equal(start, rst) and np.array_equal(sidx, rsi)
+    assert np.array_equal(spos, rsp) and np.array_equal(gcell, rgc)
+    q = np.ascontiguousarray(tgt[::64])
+    ridx = np.zeros((len(q), K), np.int32)
+    rd2 = np.zeros((len(q), K), np.float32)
+    ref.ref_knn(K, mg.P(rst), mg.P(rsi), mg.P(rsp), gw, gh, C.c_float(spacing), mg.P(q), len(q), mg.P(ridx),
+                mg.P(rd2))
+    idx, d2 = orc.Grid(gen, gw, gh, spacing).knn(q, K)
+    assert np.array_equal(idx, ridx) and np.array_equal(d2, rd2)
+    rpf, rpi = mg.run_params(spacing, 0.09, n, 1, 2.0, 300, 300)
+    stt = np.array([1, 0], np.int32)
+    sl = np.zeros(1, np.float32)
+    rgrad = np.zeros_like(gen)
+    ref.ref_loss(K, mg.P(tgt), len(tgt), mg.P(rst), mg.P(rsi), mg.P(rsp), gw, gh, C.c_float(spacing), mg.P(gen),
+                 mg.P(rgrad), mg.P(stt), mg.P(sl), mg.P(rpf), mg.P(rpi), C.c_float(1.0), C.c_uint(1))
+    g, cnt, loss = f.gradient()
+    assert cnt == int(stt[1]) and np.float32(loss) == sl[0]
+    assert np.array_equal(g, rgrad)
+    rg, rm, rv, _ = mg.ref_fit(ref, gen, tgt, K, spacing, 0.09, 1.0, 10)
+    f.step(10)
+    og, om, ov = f.generators()
+    assert np.array_equal(og, rg) and np.array_equal(om, rm) and np.array_equal(ov, rv)
 
 
 def test_cells(orc, gold):
