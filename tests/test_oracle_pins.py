@@ -220,6 +220,46 @@ def test_lattice_matches_live_reference(orc, jitter):
     assert np.array_equal(og, rg) and np.array_equal(om, rm) and np.array_equal(ov, rv)
 
 
+@pytest.mark.parametrize("jitter", [1e-6, 0.0])
+def test_lattice_cells_match_live_reference(orc, jitter):
+    """The clipper on the tie-heavy lattice (64x64 sites, jittered by 1e-6 or
+    exact: cocircular sites everywhere), with a 5-lobed occupancy, against the
+    reference's voronoiCellKernel compiled for the CPU: counts, inside flags,
+    edge labels and vertices bit for bit."""
+    if not orc.ref_available():
+        pytest.skip("the reference kernels are not compiled here")
+    from voromesh_gb300 import synth
+
+    mg = _make_golden_module()
+    ref = orc.ref()
+    gen = np.ascontiguousarray(synth.lattice(3, 5, 64, 64, jitter).reshape(-1, 2))
+    n, spacing = len(gen), float(np.float32(2.0 / 64))
+    gw, gh = orc.grid_dims(2.0, 2.0, spacing)
+    st, si, sp, _ = mg.ref_grid(ref, gen, gw, gh, spacing)
+    tiles = 16  # 128x128 voxels of size 2/128 in 8x8-voxel tiles
+    masks = np.zeros(tiles * tiles, np.uint64)
+    jj, ii = np.mgrid[0:128, 0:128]
+    x, y = (ii + 0.5) * 2 / 128 - 1, (jj + 0.5) * 2 / 128 - 1
+    occ = np.hypot(x, y) < 0.5 + 0.25 * np.cos(5 * np.arctan2(y, x))
+    for j, i in zip(*np.nonzero(occ)):
+        masks[(j >> 3) * tiles + (i >> 3)] |= np.uint64(1) << np.uint64(((j & 7) << 3) | (i & 7))
+    verts = np.zeros((n * 24, 2), np.float32)
+    edges = np.zeros(n * 24, np.int32)
+    counts = np.zeros(n, np.int32)
+    inside = np.zeros(n, np.uint8)
+    flags = np.zeros(2, np.int32)
+    ref.ref_cells(mg.P(st), mg.P(si), mg.P(sp), gw, gh, C.c_float(spacing), mg.P(gen), n, C.c_float(2.0),
+                  C.c_float(2.0), mg.P(masks), tiles, tiles, C.c_float(64.0), mg.P(verts), mg.P(edges), mg.P(counts),
+                  mg.P(inside), mg.P(flags))
+    ov, oe, oc, oi, of = orc.Grid(gen, gw, gh, spacing).cells(2.0, 2.0, masks, tiles, tiles, 64.0)
+    assert np.array_equal(oc, counts) and np.array_equal(oi, inside) and np.array_equal(of, flags)
+    assert inside.sum() > 500
+    verts, edges = verts.reshape(n, 24, 2), edges.reshape(n, 24)
+    for i in range(n):
+        c = counts[i]
+        assert np.array_equal(oe[i, :c], edges[i, :c]) and np.array_equal(ov[i, :c], verts[i, :c])
+
+
 def test_cells(orc, gold):
     from voromesh_gb300 import synth
 
