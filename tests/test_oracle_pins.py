@@ -282,3 +282,36 @@ def test_poisson(orc, gold):
     assert orc.poisson_verify(p, grid, 0, 0, p.gridW, p.gridH)
     grid, p = orc.poisson_fill(1.0, 1.0, 0.02, 30, 1, [(5, 5, 17, 13), (0, 0, 3, 40), (30, 30, 80, 80)])
     assert np.array_equal(grid, gold["poisson_regions"])
+
+
+@pytest.mark.parametrize("case", [
+    (2.0, 1.0, 0.013, 30, 5, [(10, 10, 200, 100), (50, 50, 60, 58), (0, 0, 218, 109), (-5, 30, 120, 200),
+                              (57, 3, 190, 71)]),
+    (1.0, 1.0, 0.02, 260, 2, []),
+    (1.0, 1.0, 0.3, 30, 1, [(0, 0, 2, 2)]),
+    (3.0, 2.0, 0.004, 30, 11, [(37, 53, 900, 650)]),
+    (0.5, 0.8, 0.01, 30, 10, [(3, 2, 30, 20)]),
+])
+def test_poisson_matches_live_reference(orc, case):
+    """The sampler cases the GPU tests use (non-square domains, a 4-cell grid,
+    260 rounds per call, regions off the colour grid and past the edges),
+    against the reference's dartPhaseKernel sequence compiled for the CPU:
+    the whole grid bit for bit after the fill and after every region."""
+    if not orc.ref_available():
+        pytest.skip("the reference kernels are not compiled here")
+    w, h, r, trials, seed, regions = case
+    ref = orc.ref()
+    cs = C.c_float()
+    gw, gh = C.c_int(), C.c_int()
+    ref.ref_poisson_dims(C.c_float(w), C.c_float(h), C.c_float(r), C.byref(cs), C.byref(gw), C.byref(gh))
+    grid = np.full((gw.value * gh.value, 2), -1.0, np.float32)
+    base = 0
+    for k, (x0, y0, x1, y1) in enumerate([(0, 0, gw.value, gh.value)] + list(regions)):
+        x0, y0, x1, y1 = max(x0, 0), max(y0, 0), min(x1, gw.value), min(y1, gh.value)
+        if x0 < x1 and y0 < y1:
+            ref.ref_poisson_resample(orc.P(grid), C.c_float(w), C.c_float(h), C.c_float(r), cs, gw, gh,
+                                     C.c_uint(seed), x0, y0, x1, y1, trials, C.c_uint(base))
+        base += trials
+        cells, p = orc.poisson_fill(w, h, r, trials, seed, regions[:k])
+        assert (p.gridW, p.gridH) == (gw.value, gh.value)
+        assert np.array_equal(cells, grid), f"after call {k}"
