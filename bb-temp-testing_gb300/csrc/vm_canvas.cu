@@ -266,31 +266,35 @@ __device__ __forceinline__ void float_split(float v, bool &neg, unsigned &M, int
 // double: the reference's sample-order double sum (canvas.cpp:13-25) equals
 // the 64-bit integer sum of the multiples times Q. Otherwise the samples are
 // summed in double in sample order.
+//
+// A term is at most 2^52 (M < 2^24 shifted by at most 28), and accumulation
+// stops as soon as a magnitude sum passes 2^52: every sum stays below 2^53,
+// so none can wrap, however many samples a voxel holds.
 struct RunSums {
     long long sx = 0, sy = 0;
     unsigned long long ax = 0, ay = 0;
     bool big = false;
-    __device__ void add(const float4 &q, int ex, int ey)
+    __device__ void add_axis(float v, int e0, long long &s, unsigned long long &a)
     {
         bool sg;
         unsigned M;
         int e;
-        float_split(q.x, sg, M, e);
-        if (M) {
-            int sh = e - ex;
-            big |= sh > 28;
-            unsigned long long t = sh > 28 ? 0ull : (unsigned long long)M << sh;
-            sx += sg ? -(long long)t : (long long)t;
-            ax += t;
+        float_split(v, sg, M, e);
+        if (!M || big) return;
+        const int sh = e - e0;
+        if (sh > 28) {
+            big = true;
+            return;
         }
-        float_split(q.y, sg, M, e);
-        if (M) {
-            int sh = e - ey;
-            big |= sh > 28;
-            unsigned long long t = sh > 28 ? 0ull : (unsigned long long)M << sh;
-            sy += sg ? -(long long)t : (long long)t;
-            ay += t;
-        }
+        const unsigned long long t = (unsigned long long)M << sh;
+        s += sg ? -(long long)t : (long long)t;
+        a += t;
+        if (a > (1ull << 52)) big = true;
+    }
+    __device__ void add(const float4 &q, int ex, int ey)
+    {
+        add_axis(q.x, ex, sx, ax);
+        add_axis(q.y, ey, sy, ay);
     }
     __device__ float2 mean(const float4 *__restrict__ rec, const int *__restrict__ run, int n, int ex, int ey) const
     {

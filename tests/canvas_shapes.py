@@ -29,6 +29,13 @@ def shapes():
     yield "clockwise_square", (16.0, 16.0, 0.5), np.array([[2, 2], [2, 12], [12, 12], [12, 2]], np.float32)
     yield "sliver", (16.0, 16.0, 1.0), np.array([[1, 8], [15, 8.0001], [15, 8.0002], [1, 8.0003]], np.float32)
     yield "random_poly", (50.0, 40.0, 0.7), np.random.default_rng(3).uniform(-5, 55, (40, 2)).astype(np.float32)
+    # one tile: a vertex at 1.5 * 2^-20 and 7,279 copies of (288, 288), so the
+    # voxel of (288, 288) holds ~7,284 samples each 2^28 times the tile's
+    # smallest: their integer magnitude sum needs 65 bits and, taken modulo
+    # 2^64, would pass the exact-sum certificate; the ordered double sum must
+    # decide
+    tiny = np.float32(1.5 * 2.0 ** -20)
+    yield "wrap_voxel", (512.0, 512.0, 64.0), np.array([[tiny, tiny]] + [[288.0, 288.0]] * 7279, np.float32)
 
 
 def shape(name):
@@ -37,4 +44,4 @@ def shape(name):
 
 # static, so that collecting the tests imports nothing of the package
 NAMES = ["heart_1k", "heart_small_domain", "odd_grid", "triangle_outside", "tiny_ring", "comb", "tiny_coords",
-         "single_vertex", "grid_aligned", "pentagram", "clockwise_square", "sliver", "random_poly"]
+         "single_vertex", "grid_aligned", "pentagram", "clockwise_square", "sliver", "random_poly", "wrap_voxel"]
