@@ -656,6 +656,13 @@ int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result 
                 }
                 break;
             }
+            if (rc == VM_ERR_ARG || rc == VM_ERR_UNSUPPORTED) { // a bad request: rejected, the rest served
+                res[r].status = rc;
+                res[r].finished = now();
+                ++done;
+                ++head;
+                continue;
+            }
             if (rc) {
                 vmb_destroy(b);
                 return rc;

@@ -106,3 +106,20 @@ def test_serve_target_cap(vm):
                 assert r.admitted[b] >= r.finished[a] or r.admitted[a] >= r.finished[b]
     for spec, g in zip(specs, r.generators):
         assert np.array_equal(g, alone(spec, 20))
+
+
+def test_serve_rejects_a_bad_request_and_serves_the_rest(vm):
+    """A request the batch cannot take (an unsupported lossK) gets that status;
+    the other requests are served as if it had not been sent."""
+    import dataclasses
+
+    from voromesh_gb300.batch import serve
+
+    specs = small_batch(5, seed=9)
+    specs[2] = dataclasses.replace(specs[2], lossK=7)
+    arrivals = np.linspace(0.0, 0.02, len(specs))
+    r = serve(specs, arrivals, hbm_budget=1 << 30, max_live=64, steps_per_round=10, max_steps=20, rel_tol=0.0)
+    assert r.status[2] == 7 and r.steps[2] == 0
+    for i, (spec, g) in enumerate(zip(specs, r.generators)):
+        if i != 2:
+            assert r.status[i] == 0 and np.array_equal(g, alone(spec, 20))
