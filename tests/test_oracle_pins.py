@@ -220,6 +220,43 @@ def test_lattice_matches_live_reference(orc, jitter):
     assert np.array_equal(og, rg) and np.array_equal(om, rm) and np.array_equal(ov, rv)
 
 
+def _fit_case(name):
+    from voromesh_gb300 import synth
+
+    if name == "far_targets_k16":  # generators in the middle only: the exact ring-search path
+        gen = synth.uniform(4, 1, 600, -0.5, 0.5)
+        tgt = np.concatenate([synth.circle(4, 2, 3000, 0.9, 0.05), synth.uniform(4, 3, 500, -1.2, 1.2)])
+        return gen, tgt, 0.05, 16, 1.0
+    if name == "subsampled_k16":
+        return synth.uniform(3, 1, 1024), synth.circle(3, 2, 8192, 0.6, 1e-3), 0.06, 16, 0.2
+    if name == "lattice_k12":
+        return (synth.lattice(3, 5, 64, 64, 1e-6).reshape(-1, 2), synth.five_arm_star(3, 6, 40000), 2.0 / 64, 12,
+                1.0)
+    raise KeyError(name)
+
+
+@pytest.mark.parametrize("name", ["far_targets_k16", "subsampled_k16", "lattice_k12"])
+def test_fits_match_live_reference(orc, name):
+    """Fits the GPU parity tests use beyond the plain one: targets far from
+    every generator, a 0.2 sample fraction, and k = 12 on a jittered lattice.
+    Ten steps of the reference's kernels compiled for the CPU (losses,
+    positions, moments) against the oracle in reference mode."""
+    if not orc.ref_available():
+        pytest.skip("the reference kernels are not compiled here")
+    mg = _make_golden_module()
+    gen, tgt, spacing, K, frac = _fit_case(name)
+    gen, tgt = np.ascontiguousarray(gen, np.float32), np.ascontiguousarray(tgt, np.float32)
+    spacing = float(np.float32(spacing))
+    rg, rm, rv, rloss = mg.ref_fit(orc.ref(), gen, tgt, K, spacing, 0.09, frac, 10)
+    f = orc.Fit(2.0, 2.0, spacing, K, 0.09, frac, 300, acc=orc.ACC_REF, pow_mode=orc.POW_REF, nthreads=4)
+    f.set_targets(tgt)
+    f.set_generators(gen, len(gen), 1, 2.0)
+    losses = [f.step(1) for _ in range(10)]
+    og, om, ov = f.generators()
+    assert np.array_equal(np.float32(losses), rloss)
+    assert np.array_equal(og, rg) and np.array_equal(om, rm) and np.array_equal(ov, rv)
+
+
 @pytest.mark.parametrize("jitter", [1e-6, 0.0])
 def test_lattice_cells_match_live_reference(orc, jitter):
     """The clipper on the tie-heavy lattice (64x64 sites, jittered by 1e-6 or
