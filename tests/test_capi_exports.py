@@ -113,3 +113,27 @@ def test_header_self_contained(header, tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only",
                         f"-I{ROOT / 'include'}", str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def _method_names(text, public_only):
+    """Capitalised names followed by '(' (the reference's method style); with
+    public_only, only those before the first private section."""
+    text = re.sub(r"//.*", "", text)
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    if public_only:
+        text = text.split("private:")[0]
+    return set(re.findall(r"\b([A-Z][A-Za-z0-9]*)\s*\(", text))
+
+
+@pytest.mark.parametrize("header", ["voromesh/voro_optimizer.h", "voromesh/canvas.h", "poisson/poisson_disk.h"])
+def test_reference_public_api_is_complete(header):
+    """Every public method the reference's header declares is declared in this
+    library's header of the same name (where the reference sources are
+    present)."""
+    import __graft_entry__ as g
+
+    ref = Path(g.REFERENCE_SOURCES) / "include" / header
+    if not ref.exists():
+        pytest.skip("the reference sources are not present")
+    missing = _method_names(ref.read_text(), True) - _method_names((ROOT / "include" / header).read_text(), False)
+    assert not missing, sorted(missing)
