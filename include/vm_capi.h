@@ -1,10 +1,12 @@
 /*
- * vm_capi.h — C ABI of libvoromesh_gb300.so: the GB300 VoroMesh optimiser,
- * Voronoi extraction and Poisson-disk sampler.
+ * vm_capi.h — C ABI of libvoromesh_gb300.so: the GB300 VoroMesh optimiser
+ * (vm_*), Voronoi extraction, the Poisson-disk sampler (pd_*), the voxel
+ * canvas (cv_*), and many fits at once (vmb_* batches, vms_serve).
  *
- * The reference exposes this path as two C++ classes
- * (voromesh::VoroOptimizer, include/voromesh/voro_optimizer.h:70-138, and
- * poisson::Sampler, include/poisson/poisson_disk.h:21-62). Each vm_* / pd_*
+ * The reference exposes this path as C++ classes
+ * (voromesh::VoroOptimizer, include/voromesh/voro_optimizer.h:70-138,
+ * poisson::Sampler, include/poisson/poisson_disk.h:21-62, and the host-side
+ * voromesh::Canvas, include/voromesh/canvas.h:25-89). Each vm_* / pd_* / cv_*
  * entry point below is one of their methods, flattened to plain pointers and
  * sizes: float pairs are (x, y) interleaved like Vec2 / Sample / float2, and
  * every host buffer is copied before the call returns, as the reference's
