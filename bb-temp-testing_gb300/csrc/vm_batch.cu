@@ -304,7 +304,7 @@ size_t vmb_fit_bytes(int slotsW, int slotsH, int nTargets, float width, float he
     size_t gw = std::max(1, (int)std::ceil(width / spacing)), gh = std::max(1, (int)std::ceil(height / spacing));
     size_t cells = gw * gh, tiles = (cells + kScanTile - 1) / kScanTile;
     n = std::max<size_t>(n, 1);
-    return aligned(8 * n) * 3 + aligned(16 * n) + aligned(4 * n) * 3 + aligned(8 * n) + aligned(4 * (cells + 1)) * 2 +
+    return aligned(8 * n) * 3 + aligned(8 * kGradWords * n) + aligned(4 * n) * 3 + aligned(8 * n) + aligned(4 * (cells + 1)) * 2 +
            aligned(4 * (tiles + 1)) + aligned(8 * cap) * 2 + aligned(4 * cap) * 3 + 8 * cap /* queue share */;
 }
 
@@ -354,7 +354,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     f.cap = std::max(in->nTargets, 1);
     // ---- memory: all-or-nothing from the arena
     size_t nn = std::max(n, 1);
-    size_t sizes[] = {8 * nn, 8 * nn, 8 * nn, 16 * nn, 4 * nn, 4 * nn, 4 * nn, 8 * nn, 4 * ((size_t)f.cells + 1),
+    size_t sizes[] = {8 * nn, 8 * nn, 8 * nn, 8 * kGradWords * nn, 4 * nn, 4 * nn, 4 * nn, 8 * nn, 4 * ((size_t)f.cells + 1),
                       4 * ((size_t)f.cells + 1), 4 * ((size_t)f.tiles + 1), 8 * (size_t)f.cap, 4 * (size_t)f.cap,
                       4 * (size_t)f.cap, 8 * (size_t)f.cap, 4 * (size_t)f.cap};
     char *ptrs[16];
@@ -423,7 +423,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     if ((n && ((e = cudaMemcpyAsync(D.gen, in->generators, sizeof(float2) * n, cudaMemcpyHostToDevice, b->stream)) ||
                (e = cudaMemsetAsync(D.m, 0, 8 * (size_t)n, b->stream)) ||
                (e = cudaMemsetAsync(D.v, 0, 8 * (size_t)n, b->stream)) ||
-               (e = cudaMemsetAsync(D.gradX, 0, 16 * (size_t)n, b->stream)))) ||
+               (e = cudaMemsetAsync(D.gradX, 0, 8 * kGradWords * (size_t)n, b->stream)))) ||
         (e = cudaMemsetAsync(D.counts, 0, 4 * ((size_t)f.cells + 1), b->stream)) ||
         (e = cudaMemsetAsync(D.state, 0, sizeof(VmState), b->stream)) ||
         (e = cudaMemsetAsync(f.traw, 0xFF, 8 * (size_t)f.cap, b->stream)) ||

@@ -7,6 +7,7 @@
 #pragma once
 
 #include <cfloat>
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -53,11 +54,17 @@ __device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) 
 
 // round-half-even(v * 2^e) as int64, saturating at +-2^62, NaN -> 0; integer
 // operations only (64-bit float->int conversions run on the narrow FP64 pipe).
-static __device__ __noinline__ long long fx_from_float_any(float v, int e)
+// A saturated term (|v| 2^e >= 2^62: near-coincident sites) is counted in
+// *clamped when that pointer is given.
+static __device__ __noinline__ long long fx_from_float_any(float v, int e, int *clamped)
 {
     unsigned u = __float_as_uint(v);
     int ex = (int)((u >> 23) & 0xFFu);
-    if (ex == 0xFF) return (u & 0x7FFFFFu) ? 0 : ((u >> 31) ? -4611686018427387904LL : 4611686018427387904LL);
+    if (ex == 0xFF) {
+        if (u & 0x7FFFFFu) return 0;
+        if (clamped) atomicAdd(clamped, 1);
+        return (u >> 31) ? -4611686018427387904LL : 4611686018427387904LL;
+    }
     unsigned m = u & 0x7FFFFFu;
     int k; // |v| 2^e = m 2^k
     if (ex == 0) { // subnormal v
@@ -69,6 +76,7 @@ static __device__ __noinline__ long long fx_from_float_any(float v, int e)
     }
     long long mag;
     if (k >= 0) {
+        if (k > 38 && clamped) atomicAdd(clamped, 1);
         mag = k > 38 ? 4611686018427387904LL : ((long long)m << k);
     } else if (k < -24) {
         mag = 0;
@@ -85,7 +93,7 @@ static __device__ __noinline__ long long fx_from_float_any(float v, int e)
 
 // The same with the common case inline: a normal v whose scaled value is an
 // integer below 2^62 (a plain shift of the significand, no rounding).
-__device__ __forceinline__ long long fx_from_float(float v, int e)
+__device__ __forceinline__ long long fx_from_float(float v, int e, int *clamped = nullptr)
 {
     unsigned u = __float_as_uint(v);
     int ex = (int)((u >> 23) & 0xFFu);
@@ -94,10 +102,114 @@ __device__ __forceinline__ long long fx_from_float(float v, int e)
         long long mag = (long long)((u & 0x7FFFFFu) | 0x800000u) << k;
         return (u >> 31) ? -mag : mag;
     }
-    return fx_from_float_any(v, e);
+    return fx_from_float_any(v, e, clamped);
 }
 
 __device__ __forceinline__ float fx_to_float(long long v, int e) { return __ll2float_rn(v) * pow2f(-e); }
+
+// ---- exact per-site gradient sums ----------------------------------------------
+// A site's gradient component is the exact integer sum S of int64
+// contributions x (|x| < 2^63). Each x is split as x = hi * 2^32 + lo with
+// lo = x mod 2^32 in [0, 2^32) and hi = x >> 32 (arithmetic), and the site
+// keeps L = sum(lo) (unsigned) and H = sum(hi) (signed) in two 64-bit words.
+// A site receives fewer than 2^31 contributions (one per target at most), so
+// L < 2^63 and |H| < 2^62: neither word wraps and S = H * 2^32 + L exactly,
+// for any input, where one 64-bit sum would wrap past 2^63. Per slot the
+// words are laid out as {Lx, Ly, Hx, Hy} (kGradWords per slot).
+
+__host__ __device__ __forceinline__ float vm_pow2f(int e)
+{
+#ifdef __CUDA_ARCH__
+    return __int_as_float((e + 127) << 23);
+#else
+    return ldexpf(1.0f, e);
+#endif
+}
+
+__host__ __device__ __forceinline__ float vm_u64_to_float(unsigned long long v)
+{
+#ifdef __CUDA_ARCH__
+    return __ull2float_rn(v);
+#else
+    return (float)v;
+#endif
+}
+
+__host__ __device__ __forceinline__ float vm_s64_to_float(long long v)
+{
+#ifdef __CUDA_ARCH__
+    return __ll2float_rn(v);
+#else
+    return (float)v;
+#endif
+}
+
+// S * 2^-e rounded once to float when |S| >= 2^63 (T = S >> 32 outside the
+// int32 range, low = S mod 2^32): the 128-bit magnitude is shifted so its
+// leading one is bit 63 of a 64-bit word, the bits shifted out are folded
+// into bit 0 as a sticky bit (far below the rounding position), and the word
+// is converted with round-to-nearest-even and scaled back by a power of two.
+__host__ __device__ __noinline__ inline float fx2_to_float_wide(long long T, unsigned long long low, int e)
+{
+    unsigned long long lo = ((unsigned long long)T << 32) | low;
+    unsigned long long hi = (unsigned long long)(T >> 32);
+    bool neg = T < 0;
+    if (neg) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    }
+    float f;
+    if (hi == 0) {
+        f = vm_u64_to_float(lo);
+    } else {
+#ifdef __CUDA_ARCH__
+        int c = __clzll((long long)hi);
+#else
+        int c = __builtin_clzll(hi);
+#endif
+        // |S| < 2^95, so hi < 2^31 and c is in [33, 63]
+        unsigned long long top = (hi << c) | (lo >> (64 - c));
+        unsigned long long rest = lo << c;
+        top |= rest != 0 ? 1ull : 0ull;
+        f = vm_u64_to_float(top) * vm_pow2f(64 - c);
+    }
+    if (neg) f = -f;
+    return f * vm_pow2f(-e);
+}
+
+// S * 2^-e, S = H * 2^32 + L, rounded once to float (the same value as
+// converting S exactly and scaling, which is what (float)S * 2^-e gives when
+// S fits an int64).
+__host__ __device__ __forceinline__ float fx2_to_float(long long H, unsigned long long L, int e)
+{
+    long long T = H + (long long)(L >> 32); // S = T * 2^32 + (L mod 2^32)
+    unsigned long long low = L & 0xFFFFFFFFull;
+    if (T >= -2147483648LL && T <= 2147483647LL)
+        return vm_s64_to_float((long long)(((unsigned long long)T << 32) | low)) * vm_pow2f(-e);
+    return fx2_to_float_wide(T, low, e);
+}
+
+// Adds contributions x, y to the split words of site s (G: kGradWords per slot).
+__device__ __forceinline__ void fx2_red(unsigned long long *G, int s, long long x, long long y)
+{
+    unsigned long long *g = G + (size_t)kGradWords * s;
+    if (x) {
+        atomicAdd(&g[0], (unsigned long long)x & 0xFFFFFFFFull);
+        long long h = x >> 32;
+        if (h) atomicAdd(&g[2], (unsigned long long)h);
+    }
+    if (y) {
+        atomicAdd(&g[1], (unsigned long long)y & 0xFFFFFFFFull);
+        long long h = y >> 32;
+        if (h) atomicAdd(&g[3], (unsigned long long)h);
+    }
+}
+
+// |v| < 2^62: a further term (|x| <= 2^62) can be added without overflow.
+__device__ __forceinline__ bool fx_small(long long v)
+{
+    return (unsigned)((int)(v >> 32) + 0x40000000) < 0x80000000u;
+}
 
 __device__ __forceinline__ void fxl_from_float(float v, int e, unsigned long long &lo, unsigned long long &hi)
 {

@@ -525,8 +525,10 @@ __device__ __forceinline__ void load_fit(const VmFit *__restrict__ fits, int f, 
 
 // A lane's running gradient sum for one site: consecutive targets of a lane
 // mostly share their nearest site and bisector neighbour, so the sum reaches
-// the fit's accumulator only when the site changes (one 64-bit reduction per
-// component; integer sums, so the grouping does not change the result).
+// the fit's split accumulators only when the site changes (integer sums, so
+// the grouping does not change the result). A running sum is also flushed
+// before it could overflow: terms are at most 2^62 in magnitude, so a sum
+// below 2^62 takes one more term safely.
 struct RunSum {
     int site = -1;
     long long x = 0, y = 0;
@@ -534,17 +536,14 @@ struct RunSum {
 
 __device__ __forceinline__ void run_flush(RunSum &r, unsigned long long *G)
 {
-    if (r.site >= 0) {
-        if (r.x) atomicAdd(&G[2 * (size_t)r.site], (unsigned long long)r.x);
-        if (r.y) atomicAdd(&G[2 * (size_t)r.site + 1], (unsigned long long)r.y);
-    }
+    if (r.site >= 0) fx2_red(G, r.site, r.x, r.y);
     r.site = -1;
     r.x = r.y = 0;
 }
 
 __device__ __forceinline__ void run_add(RunSum &r, int site, long long x, long long y, unsigned long long *G)
 {
-    if (site != r.site) {
+    if (site != r.site || !fx_small(r.x) || !fx_small(r.y)) {
         run_flush(r, G);
         r.site = site;
     }
@@ -683,8 +682,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 aCnt += 1;
                 if (mode == 0) {
                     int e = F.gradExp;
-                    run_add(run0, o.i0, fx_from_float(o.g0x, e), fx_from_float(o.g0y, e), G);
-                    run_add(runJ, o.j, fx_from_float(o.gjx, e), fx_from_float(o.gjy, e), G);
+                    int *cl = &F.state->clamped;
+                    run_add(run0, o.i0, fx_from_float(o.g0x, e, cl), fx_from_float(o.g0y, e, cl), G);
+                    run_add(runJ, o.j, fx_from_float(o.gjx, e, cl), fx_from_float(o.gjy, e, cl), G);
                 }
             }
         }
@@ -752,11 +752,10 @@ __global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fi
         atomicAdd(&F.state->accCount, 1);
         if (mode == 0) {
             int e = F.gradExp;
+            int *cl = &F.state->clamped;
             unsigned long long *g = reinterpret_cast<unsigned long long *>(F.gradX);
-            atomicAdd(&g[2 * (size_t)o.j], (unsigned long long)fx_from_float(o.gjx, e));
-            atomicAdd(&g[2 * (size_t)o.j + 1], (unsigned long long)fx_from_float(o.gjy, e));
-            atomicAdd(&g[2 * (size_t)o.i0], (unsigned long long)fx_from_float(o.g0x, e));
-            atomicAdd(&g[2 * (size_t)o.i0 + 1], (unsigned long long)fx_from_float(o.g0y, e));
+            fx2_red(g, o.j, fx_from_float(o.gjx, e, cl), fx_from_float(o.gjy, e, cl));
+            fx2_red(g, o.i0, fx_from_float(o.g0x, e, cl), fx_from_float(o.g0y, e, cl));
         }
     }
 }

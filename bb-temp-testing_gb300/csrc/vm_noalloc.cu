@@ -13,9 +13,13 @@
 // The first call on a device looks up that array's device address with
 // cudaGetSymbolAddress (the array's name in host code is only a host-side
 // stand-in, not a device address); make that first call before any stream
-// capture. Every call shares the array, so calls that overlap on the GPU
-// (different streams, or different host threads) race and must be ordered
-// by the caller. Each call clears the counts it uses before binning.
+// capture: a first call on a capturing stream returns VM_ERR_UNSUPPORTED
+// instead of invalidating the capture. The address is kept for the process;
+// a cudaDeviceReset reloads the library's module and invalidates it, so a
+// failed launch drops it and the next call looks it up again. Every call
+// shares the array, so calls that overlap on the GPU (different streams, or
+// different host threads) race and must be ordered by the caller. Each call
+// clears the counts it uses before binning.
 #include <cstddef>
 #include <mutex>
 
@@ -49,10 +53,16 @@ char *g_scratchAddr[kMaxDevices]; // device address of g_noallocScratch, per dev
 std::mutex g_scratchMutex;
 
 // Per-device set-up with that device current: the device address of the array.
-int scratch_for(int dev, char **out)
+int scratch_for(int dev, cudaStream_t s, char **out)
 {
     std::lock_guard<std::mutex> lock(g_scratchMutex);
     if (!g_scratchAddr[dev]) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaError_t ce = cudaStreamIsCapturing(s, &cs);
+        if (ce != cudaSuccess) return vmh::cuda_fail(ce, "cudaStreamIsCapturing");
+        if (cs != cudaStreamCaptureStatusNone)
+            return vmh::fail(VM_ERR_UNSUPPORTED, "vm_build_grid_noalloc: the first call on a device must come "
+                                                 "before any stream capture");
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
         if (e != cudaSuccess) return vmh::cuda_fail(e, "cudaGetSymbolAddress");
@@ -60,6 +70,12 @@ int scratch_for(int dev, char **out)
     }
     *out = g_scratchAddr[dev];
     return VM_OK;
+}
+
+void scratch_forget(int dev)
+{
+    std::lock_guard<std::mutex> lock(g_scratchMutex);
+    g_scratchAddr[dev] = nullptr;
 }
 
 } // namespace
@@ -76,10 +92,13 @@ extern "C" int vm_build_grid_noalloc(const float *generators, int n, int gridW, 
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return vmh::cuda_fail(e, "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) return vmh::fail(VM_ERR_UNSUPPORTED, "vm_build_grid_noalloc: device index too large");
-    char *base = nullptr;
-    int rc = scratch_for(dev, &base);
-    if (rc) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    char *base = nullptr;
+    int rc = scratch_for(dev, s, &base);
+    if (rc) return rc;
+    // a non-sticky error left pending by earlier, unrelated work is cleared
+    // here so that it is not reported as this call's failure
+    (void)cudaGetLastError();
     int cells = gridW * gridH;
     int tiles = (cells + kScanTile - 1) / kScanTile;
     VmPointSet S{};
@@ -101,11 +120,25 @@ extern "C" int vm_build_grid_noalloc(const float *generators, int n, int gridW, 
     if ((e = cudaMemsetAsync(S.counts, 0, sizeof(int) * (size_t)(cells + 1), s)) != cudaSuccess)
         return vmh::cuda_fail(e, "clear counts");
     int blocks = (n + 255) / 256;
-    if (blocks) k_na_bin<<<blocks, 256, 0, s>>>(S);
+    // each launch is checked before the next is enqueued
+    auto launched = [&](const char *what) -> int {
+        cudaError_t le = cudaGetLastError();
+        if (le == cudaSuccess) return VM_OK;
+        scratch_forget(dev);
+        return vmh::cuda_fail(le, what);
+    };
+    if (blocks) {
+        k_na_bin<<<blocks, 256, 0, s>>>(S);
+        if ((rc = launched("vm_build_grid_noalloc: bin"))) return rc;
+    }
     k_na_tile_sum<<<tiles, 256, 0, s>>>(S);
+    if ((rc = launched("vm_build_grid_noalloc: tile sums"))) return rc;
     k_na_tile_apply<<<tiles, 256, 0, s>>>(S);
-    if (blocks) k_na_scatter<<<blocks, 256, 0, s>>>(S);
+    if ((rc = launched("vm_build_grid_noalloc: scan"))) return rc;
+    if (blocks) {
+        k_na_scatter<<<blocks, 256, 0, s>>>(S);
+        if ((rc = launched("vm_build_grid_noalloc: scatter"))) return rc;
+    }
     k_na_canonical<<<(cells + 255) / 256, 256, 0, s>>>(S);
-    if ((e = cudaGetLastError()) != cudaSuccess) return vmh::cuda_fail(e, "vm_build_grid_noalloc launch");
-    return VM_OK;
+    return launched("vm_build_grid_noalloc: canonical order");
 }

@@ -16,6 +16,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include "vm_capi.h"
+#include "vm_device.cuh"
 #include "vm_host.h"
 #include "vm_kernels.h"
 
@@ -132,6 +133,7 @@ struct vm_optimizer {
     VmFit fit{};
     MeshHost mesh;
     long long exactTotal = 0;
+    long long clampedTotal = 0; // gradient terms clamped to +-2^62 in fixed point
 
     int numSlots() const { return slotsW * slotsH; }
 };
@@ -269,7 +271,7 @@ int autotune_loss_variant(vm_optimizer *h)
             score[v] = std::min(score[v], ms);
         }
     int best = (int)(std::min_element(score.begin(), score.end()) - score.begin());
-    if ((e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * 2 * (size_t)h->numSlots(), h->stream)) ||
+    if ((e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * kGradWords * (size_t)h->numSlots(), h->stream)) ||
         (e = cudaMemcpyAsync(h->state.p, &saved, sizeof(VmState), cudaMemcpyHostToDevice, h->stream)) ||
         (e = cudaStreamSynchronize(h->stream)))
         return cuda_fail(e, "tune restore");
@@ -641,7 +643,7 @@ int vm_set_generators(vm_optimizer *h, const float *xy, int slotsW, int slotsH, 
         drop_graph(h);
         h->slotsW = slotsW;
         h->slotsH = slotsH;
-        if ((rc = h->gen.alloc(n)) || (rc = h->m.alloc(n)) || (rc = h->v.alloc(n)) || (rc = h->gradX.alloc(2 * (size_t)n)) ||
+        if ((rc = h->gen.alloc(n)) || (rc = h->m.alloc(n)) || (rc = h->v.alloc(n)) || (rc = h->gradX.alloc(kGradWords * (size_t)n)) ||
             (rc = h->key.alloc(n)) || (rc = h->rank.alloc(n)) || (rc = h->sortedIdx.alloc(n)) ||
             (rc = h->sortedPos.alloc(n)))
             return rc;
@@ -654,7 +656,7 @@ int vm_set_generators(vm_optimizer *h, const float *xy, int slotsW, int slotsH, 
     cudaError_t e;
     if (n > 0) {
         if ((e = cudaMemcpyAsync(h->gen.p, xy, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, h->stream)) ||
-            (e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * 2 * (size_t)n, h->stream)))
+            (e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * kGradWords * (size_t)n, h->stream)))
             return cuda_fail(e, "upload generators");
     }
     h->gridValid = false;
@@ -741,6 +743,7 @@ int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
     h->iteration = st.iter;
     h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
     h->exactTotal = st.slowTotal;
+    h->clampedTotal = st.clamped;
     float ms = 0.0f;
     if ((e = cudaEventElapsedTime(&ms, h->ev0, h->ev1))) return cuda_fail(e, "elapsed");
     if (gpuMs) *gpuMs = ms;
@@ -783,6 +786,7 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
     h->iteration = st.iter;
     h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
     h->exactTotal = st.slowTotal;
+    h->clampedTotal = st.clamped;
     for (int k = 0; k < iterations; ++k) {
         cudaEvent_t *ev = &h->timing[(size_t)k * 5];
         for (int j = 0; j < 4; ++j) {
@@ -845,6 +849,7 @@ int vm_info(vm_optimizer *h, vm_info_t *out)
     out->gridH = h->gridH;
     out->lastBatchLoss = h->lastBatchLoss;
     out->exactTargets = h->exactTotal;
+    out->clampedTerms = h->clampedTotal;
     return VM_OK;
 }
 
@@ -943,7 +948,7 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
     }
     std::vector<int> hi0(live), hj(live), slot(live);
     std::vector<float> hl(live);
-    std::vector<long long> g(grad ? 2 * (size_t)n : 0);
+    std::vector<long long> g(grad ? kGradWords * (size_t)n : 0);
     VmState st;
     if (live > 0) {
         if ((e = cudaMemcpyAsync(hi0.data(), h->dbgI0.p, sizeof(int) * live, cudaMemcpyDeviceToHost, h->stream)) ||
@@ -952,9 +957,11 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
             (e = cudaMemcpyAsync(slot.data(), h->tslot.p, sizeof(int) * live, cudaMemcpyDeviceToHost, h->stream)))
             return cuda_fail(e, "probe read");
     }
-    if (grad && (e = cudaMemcpyAsync(g.data(), h->gradX.p, sizeof(long long) * 2 * n, cudaMemcpyDeviceToHost, h->stream)))
+    if (grad && (e = cudaMemcpyAsync(g.data(), h->gradX.p, sizeof(long long) * kGradWords * n, cudaMemcpyDeviceToHost,
+                                     h->stream)))
         return cuda_fail(e, "probe grad");
-    if ((e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * 2 * (size_t)n, h->stream))) return cuda_fail(e, "probe clear");
+    if ((e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * kGradWords * (size_t)n, h->stream)))
+        return cuda_fail(e, "probe clear");
     if ((rc = read_state(h, st))) return rc;
     h->fit = saved;
     if ((rc = upload_tables(h))) return rc;
@@ -970,8 +977,11 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
         if (loss) loss[s] = hl[t];
     }
     if (grad) {
-        float scale = std::ldexp(1.0f, -h->fit.gradExp);
-        for (size_t k = 0; k < 2 * (size_t)n; ++k) grad[k] = (float)g[k] * scale;
+        for (size_t k = 0; k < (size_t)n; ++k) {
+            const long long *w = &g[kGradWords * k]; // {Lx, Ly, Hx, Hy}
+            grad[2 * k] = vmk::fx2_to_float(w[2], (unsigned long long)w[0], h->fit.gradExp);
+            grad[2 * k + 1] = vmk::fx2_to_float(w[3], (unsigned long long)w[1], h->fit.gradExp);
+        }
     }
     if (count) *count = st.count;
     if (lossSum) *lossSum = st.loss;

@@ -108,8 +108,11 @@ __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits
     float lr = st->schedLr, bc1 = st->schedBc1, bc2 = st->schedBc2;
     int count = st->accCount;
     float scale = 1.0f / (float)(count > 1 ? count : 1);
-    longlong2 gq = reinterpret_cast<const longlong2 *>(F.gradX)[i];
-    if (gq.x | gq.y) reinterpret_cast<longlong2 *>(F.gradX)[i] = make_longlong2(0, 0);
+    // the exact split sums {Lx, Ly} {Hx, Hy} of this slot, cleared for the next step
+    longlong2 *gw = reinterpret_cast<longlong2 *>(F.gradX) + 2 * (size_t)i;
+    longlong2 gl = gw[0], gh = gw[1];
+    if (gl.x | gl.y) gw[0] = make_longlong2(0, 0);
+    if (gh.x | gh.y) gw[1] = make_longlong2(0, 0);
     float2 p = F.gen[i];
     bool inRegion = true;
     if (F.cx0 != 0 || F.cy0 != 0 || F.cx1 != F.slotsW || F.cy1 != F.slotsH) {
@@ -117,8 +120,8 @@ __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits
         inRegion = sx >= F.cx0 && sx < F.cx1 && sy >= F.cy0 && sy < F.cy1;
     }
     if (p.x >= 0.0f && inRegion) {
-        float grx = scale * fx_to_float(gq.x, F.gradExp);
-        float gry = scale * fx_to_float(gq.y, F.gradExp);
+        float grx = scale * fx2_to_float(gh.x, (unsigned long long)gl.x, F.gradExp);
+        float gry = scale * fx2_to_float(gh.y, (unsigned long long)gl.y, F.gradExp);
         float2 m = F.m[i], v = F.v[i];
         float b1 = F.beta1, b2 = F.beta2;
         float mx = b1 * m.x + (1.0f - b1) * grx;

@@ -29,7 +29,8 @@ struct VmState {
     int slowTotal;   // targets that needed the exact ring search (cumulative)
     int errors;      // error bits raised by kernels (see VM_KERR_*)
     float schedLr, schedBc1, schedBc2; // this step's learning rate and bias corrections
-    int pad[16];
+    int clamped;     // gradient terms clamped to +-2^62 in fixed point (cumulative)
+    int pad[15];
 };
 
 enum : int {
@@ -56,7 +57,7 @@ struct VmFit {
     int pad0;
     // ---- device arrays ----
     VM_F2 *gen, *m, *v;   // slot order
-    long long *gradX;     // 2 per slot, fixed point
+    long long *gradX;     // 4 per slot: exact split fixed-point sums {Lx, Ly, Hx, Hy}
     int *key, *rank;      // per slot: grid cell (-1 empty) and rank within the cell
     int *counts;          // gridW*gridH (+1): per-cell counts, zero between builds
     int *start;           // gridW*gridH + 1: cell start in the sorted arrays
@@ -86,3 +87,4 @@ struct VmPointSet {
 };
 
 constexpr int kScanTile = 2048; // cells per scan tile (256 threads x 8)
+constexpr int kGradWords = 4;   // 64-bit words of exact gradient sums per slot {Lx, Ly, Hx, Hy}

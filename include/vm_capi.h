@@ -76,6 +76,8 @@ typedef struct {
     int gridW, gridH;     /* hash grid */
     float lastBatchLoss;  /* LastBatchLoss() */
     long long exactTargets; /* targets resolved by the exact ring search so far */
+    long long clampedTerms; /* gradient terms whose fixed-point image passed +-2^62 and was clamped
+                               there (only near-coincident sites produce them); 0 in practice */
 } vm_info_t;
 
 typedef struct {
@@ -260,9 +262,11 @@ int vms_serve(const vms_request *reqs, int n, const vms_config *cfg, vms_result 
  * VM_NOALLOC_MAX_CELLS cells; larger requests return VM_ERR_ARG. Work is
  * enqueued on `stream` (a cudaStream_t, NULL = the legacy default stream)
  * and the call returns without waiting. The first call on a device sets up
- * that device's scratch address; make it before any stream capture. All
- * calls share the scratch array: calls that overlap on the GPU race, so the
- * caller must order them (one stream, or events). */
+ * that device's scratch address; make it before any stream capture (a first
+ * call on a capturing stream returns VM_ERR_UNSUPPORTED). A cudaDeviceReset
+ * invalidates that address; the next call after a failed launch looks it up
+ * again. All calls share the scratch array: calls that overlap on the GPU
+ * race, so the caller must order them (one stream, or events). */
 #define VM_NOALLOC_MAX_POINTS 262144
 #define VM_NOALLOC_MAX_CELLS 262144
 int vm_build_grid_noalloc(const float *generators, int n, int gridW, int gridH, float cellSize, int *start,

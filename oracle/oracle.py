@@ -84,6 +84,8 @@ def lib() -> C.CDLL:
         _lib.vo_fixed_loss_to_float.argtypes = [C.c_uint64, C.c_uint64, C.c_int]
         _lib.vo_fixed_to_float.restype = C.c_float
         _lib.vo_fixed_to_float.argtypes = [C.c_int64, C.c_int]
+        _lib.vo_fixed2_to_float.restype = C.c_float
+        _lib.vo_fixed2_to_float.argtypes = [C.c_int64, C.c_uint64, C.c_int]
         _lib.vo_fixed_from_float.restype = C.c_int64
         _lib.vo_fixed_from_float.argtypes = [C.c_float, C.c_int]
         _lib.vo_fixed_grad_exp.argtypes = [C.c_float]

@@ -232,6 +232,23 @@ int64_t vo_fixed_from_float(float v, int e)
 
 float vo_fixed_to_float(int64_t v, int e) { return (float)v * ldexpf(1.0f, -e); }
 
+/* Exact per-site gradient sums: each int64 term v is added to two words,
+ * L += v mod 2^32 (unsigned) and H += v >> 32 (arithmetic), so the site's sum
+ * S = H * 2^32 + L is exact for fewer than 2^31 terms, where one 64-bit sum
+ * would wrap past 2^63. S is formed in 128 bits and rounded to float once
+ * (the C conversion from __int128 rounds to nearest even), then scaled. */
+void vo_fixed2_add(int64_t v, int64_t *H, uint64_t *L)
+{
+    __atomic_fetch_add(L, (uint64_t)v & 0xFFFFFFFFull, __ATOMIC_RELAXED);
+    __atomic_fetch_add(H, v >> 32, __ATOMIC_RELAXED);
+}
+
+float vo_fixed2_to_float(int64_t H, uint64_t L, int e)
+{
+    __int128 S = (__int128)H * ((__int128)1 << 32) + (__int128)L;
+    return (float)S * ldexpf(1.0f, -e);
+}
+
 void vo_fixed_loss_add(float v, int e, uint64_t *lo, uint64_t *hi)
 {
     if (!(v > 0.0f)) return;
@@ -361,11 +378,12 @@ static void loss_fixed_range(void *ctx, int64_t lo, int64_t hi, int tid)
         ++cnt;
         vo_fixed_loss_add(o.loss, J->le, &llo, &lhi);
         if (J->gradFixed) {
-            __atomic_fetch_add(&J->gradFixed[2 * o.j], vo_fixed_from_float(o.g[0], J->ge), __ATOMIC_RELAXED);
-            __atomic_fetch_add(&J->gradFixed[2 * o.j + 1], vo_fixed_from_float(o.g[1], J->ge), __ATOMIC_RELAXED);
-            __atomic_fetch_add(&J->gradFixed[2 * o.i0], vo_fixed_from_float(o.g[2], J->ge), __ATOMIC_RELAXED);
-            __atomic_fetch_add(&J->gradFixed[2 * o.i0 + 1], vo_fixed_from_float(o.g[3], J->ge),
-                               __ATOMIC_RELAXED);
+            /* words per site: L.x, L.y, H.x, H.y */
+            int64_t *gj = J->gradFixed + 4 * (size_t)o.j, *g0 = J->gradFixed + 4 * (size_t)o.i0;
+            vo_fixed2_add(vo_fixed_from_float(o.g[0], J->ge), &gj[2], (uint64_t *)&gj[0]);
+            vo_fixed2_add(vo_fixed_from_float(o.g[1], J->ge), &gj[3], (uint64_t *)&gj[1]);
+            vo_fixed2_add(vo_fixed_from_float(o.g[2], J->ge), &g0[2], (uint64_t *)&g0[0]);
+            vo_fixed2_add(vo_fixed_from_float(o.g[3], J->ge), &g0[3], (uint64_t *)&g0[1]);
         }
     }
     J->lo[tid] = llo;
@@ -478,10 +496,10 @@ static void adam_range(void *ctx, int64_t lo, int64_t hi, int tid)
         int i = (int)ii;
         float grx, gry;
         if (J->gradFixed) {
-            grx = vo_fixed_to_float(J->gradFixed[2 * i], J->gradExp);
-            gry = vo_fixed_to_float(J->gradFixed[2 * i + 1], J->gradExp);
-            J->gradFixed[2 * i] = 0;
-            J->gradFixed[2 * i + 1] = 0;
+            int64_t *w = J->gradFixed + 4 * (size_t)i;
+            grx = vo_fixed2_to_float(w[2], (uint64_t)w[0], J->gradExp);
+            gry = vo_fixed2_to_float(w[3], (uint64_t)w[1], J->gradExp);
+            w[0] = w[1] = w[2] = w[3] = 0;
         } else {
             grx = J->gradFloat[2 * i];
             gry = J->gradFloat[2 * i + 1];
@@ -616,7 +634,7 @@ void vo_fit_set_generators(vo_fit *f, const vo_f2 *slots, int slotsW, int slotsH
         f->m = (vo_f2 *)calloc(nn, sizeof(vo_f2));
         f->v = (vo_f2 *)calloc(nn, sizeof(vo_f2));
         f->gradF = (float *)calloc(2 * nn, sizeof(float));
-        f->gradX = (int64_t *)calloc(2 * nn, sizeof(int64_t));
+        f->gradX = (int64_t *)calloc(4 * nn, sizeof(int64_t));
         f->genCell = (int *)malloc(sizeof(int) * nn);
         f->sortedIdx = (int *)malloc(sizeof(int) * nn);
         f->sortedPos = (vo_f2 *)malloc(sizeof(vo_f2) * nn);
@@ -624,7 +642,7 @@ void vo_fit_set_generators(vo_fit *f, const vo_f2 *slots, int slotsW, int slotsH
     f->slotCellSize = slotCellSize;
     if (n > 0) memcpy(f->gen, slots, sizeof(vo_f2) * (size_t)n);
     memset(f->gradF, 0, sizeof(float) * 2 * (size_t)(n > 0 ? n : 1));
-    memset(f->gradX, 0, sizeof(int64_t) * 2 * (size_t)(n > 0 ? n : 1));
+    memset(f->gradX, 0, sizeof(int64_t) * 4 * (size_t)(n > 0 ? n : 1));
     vo_fit_begin_schedule(f, f->paramIterations, 0, 0, f->slotsW, f->slotsH);
 }
 
@@ -762,11 +780,15 @@ void vo_fit_gradient(vo_fit *f, float *grad, int *count, float *loss)
         memcpy(grad, gf, sizeof(float) * 2 * (size_t)n);
         free(gf);
     } else {
-        int64_t *gx = (int64_t *)calloc(2 * (size_t)n, sizeof(int64_t));
+        int64_t *gx = (int64_t *)calloc(4 * (size_t)(n > 0 ? n : 1), sizeof(int64_t));
         vo_loss(f->targets, f->targetCapacity, &g, f->gen, n, f->K, &f->rp, f->sampleFraction, f->seed, it,
                 VO_ACC_FIXED, f->spacing, NULL, gx, &ls, f->nthreads);
         int e = vo_fixed_grad_exp(f->spacing);
-        for (int i = 0; i < 2 * n; ++i) grad[i] = vo_fixed_to_float(gx[i], e);
+        for (int i = 0; i < n; ++i) {
+            const int64_t *w = gx + 4 * (size_t)i;
+            grad[2 * i] = vo_fixed2_to_float(w[2], (uint64_t)w[0], e);
+            grad[2 * i + 1] = vo_fixed2_to_float(w[3], (uint64_t)w[1], e);
+        }
         free(gx);
     }
     *count = ls.count;

@@ -15,9 +15,10 @@
  * Two accumulation modes exist for the loss/gradient sums:
  *   VO_ACC_REF    float sums in target-index order, as a serial execution of
  *                 the reference kernel produces (its GPU order is racy);
- *   VO_ACC_FIXED  the product's order-independent fixed-point sums (int64
- *                 per gradient component, 128-bit for the loss), restated
- *                 here independently so the GPU path can be checked bit-exact.
+ *   VO_ACC_FIXED  the product's order-independent fixed-point sums (exact
+ *                 split 64-bit word pairs per gradient component, 128-bit for
+ *                 the loss), restated here independently so the GPU path can
+ *                 be checked bit-exact.
  * Two bias-correction modes exist for Adam:
  *   VO_POW_REF    powf(beta, t) (reference voro_optimizer.cu:287-288);
  *   VO_POW_DET    double exponentiation by squaring rounded to float (the
@@ -75,8 +76,9 @@ void vo_knn_brute(const vo_f2 *gen, int n, vo_f2 q, int K, int *idx, float *d2);
 /* ---- VoroLoss ----------------------------------------------------------------
  * vorolossKernel (voro_optimizer.cu:199-266) over all targets. rp may be NULL
  * (EvaluateLoss). grad (REF mode: float2[n]) or gradFixed (FIXED mode:
- * int64[2n]) may be NULL for a loss-only pass. Outputs the summed loss and
- * the number of contributing targets. nthreads > 1 only in FIXED mode. */
+ * int64[4n], per site the words L.x, L.y, H.x, H.y of vo_fixed2_add) may be
+ * NULL for a loss-only pass. Outputs the summed loss and the number of
+ * contributing targets. nthreads > 1 only in FIXED mode. */
 typedef struct {
     float loss;      /* float sum (REF) or the rounded fixed-point sum (FIXED) */
     int count;
@@ -98,12 +100,16 @@ int vo_fixed_grad_exp(float spacing);
 int vo_fixed_loss_exp(float spacing);
 int64_t vo_fixed_from_float(float v, int e);
 float vo_fixed_to_float(int64_t v, int e);
+/* exact split sums: add v to (H, L); S = H * 2^32 + L rounded once to float, times 2^-e */
+void vo_fixed2_add(int64_t v, int64_t *H, uint64_t *L);
+float vo_fixed2_to_float(int64_t H, uint64_t L, int e);
 void vo_fixed_loss_add(float v, int e, uint64_t *lo, uint64_t *hi);
 float vo_fixed_loss_to_float(uint64_t lo, uint64_t hi, int e);
 
 /* ---- Adam --------------------------------------------------------------------
  * adamKernel (voro_optimizer.cu:271-301). gradFloat (REF) or gradFixed
- * (FIXED, converted with vo_fixed_to_float) is read and zeroed. */
+ * (FIXED, 4 words per site, converted with vo_fixed2_to_float) is read and
+ * zeroed. */
 float vo_pow_det(float base, int t);
 void vo_adam(vo_f2 *gen, vo_f2 *m, vo_f2 *v, float *gradFloat, int64_t *gradFixed, int gradExp, int n,
              int iter, int count, const vo_run_params *rp, int powMode, int nthreads);

@@ -200,3 +200,41 @@ def test_steps_after_every_target_is_removed(vm, orc):
         om, ov = opt.Moments()
         assert np.array_equal(om, m) and np.array_equal(ov, v)
     assert opt.info().liveTargets == 0
+
+
+def _one_sided_fit():
+    """Three sites and 2^20 targets in a small cluster far to their right:
+    every target pulls the same site the same way, so the per-site gradient
+    sums reach about 2^63.8 in fixed point, past what one int64 can hold."""
+    from voromesh_gb300 import synth
+
+    gen = np.array([[0.2, 1.0], [1.0, 1.0], [1.0, 0.2]], np.float32)
+    tgt = (synth.uniform(23, 2, 1 << 20, -0.02, 0.02, shift=False) + np.float32([1.9, 1.0])).astype(np.float32)
+    return gen, tgt
+
+
+def test_gradient_sums_past_int64(vm, orc):
+    """The exact split gradient sums: the GPU gradient equals the oracle's bit
+    for bit and stays within 1e-6 of the FP64 gradient (a wrapped 64-bit sum
+    would be off by 2^64 units), and three steps of positions and moments
+    equal the oracle's."""
+    gen, tgt = _one_sided_fit()
+    opt, ref = _pair(vm, orc, gen, tgt, 0.1, 12, 0, 1.0, slots=(3, 1))
+    _, _, _, grad, cnt, _ = opt.Probe(0)
+    g, rcnt, _ = ref.gradient()
+    assert cnt == rcnt == len(tgt)
+    assert np.array_equal(grad, g)
+    d = orc.Fit64(2.0, 2.0, float(np.float32(0.1)), 12, 0.09, 1.0, 300)
+    d.set_targets(tgt)
+    d.set_generators(gen, 3, 1, 2.0)
+    g64, _, _ = d.gradient()
+    e = orc.lib().vo_fixed_grad_exp(np.float32(0.1))
+    assert np.log2(np.abs(g64).max()) + e > 63.5  # the sums do pass 2^63
+    assert np.abs(grad - g64).max() <= 1e-6 * np.abs(g64).max()
+    opt.Step(3)
+    ref.step(3)
+    rg, rm, rv = ref.generators()
+    om, ov = opt.Moments()
+    assert np.array_equal(opt.Generators(), rg)
+    assert np.array_equal(om, rm) and np.array_equal(ov, rv)
+    assert opt.info().clampedTerms == 0

@@ -352,3 +352,63 @@ def test_poisson_matches_live_reference(orc, case):
         cells, p = orc.poisson_fill(w, h, r, trials, seed, regions[:k])
         assert (p.gridW, p.gridH) == (gw.value, gh.value)
         assert np.array_equal(cells, grid), f"after call {k}"
+
+
+def _f32_round(num: int, e: int) -> np.float32:
+    """num * 2^-e rounded to the nearest float32 (ties to even), from exact integers."""
+    if num == 0:
+        return np.float32(0.0)
+    sign = -1 if num < 0 else 1
+    a = abs(num)
+    shift = a.bit_length() - 24
+    if shift > 0:
+        q, r = divmod(a, 1 << shift)
+        half = 1 << (shift - 1)
+        if r > half or (r == half and q & 1):
+            q += 1
+        a, e = q, e - shift
+    return np.float32(sign * np.ldexp(float(a), -e))
+
+
+def test_split_sum_rounding(orc):
+    """vo_fixed2_to_float: S = H * 2^32 + L rounded once to float, on both
+    sides of the int64 range, with ties and sticky bits below the rounding
+    position."""
+    rng = np.random.default_rng(5)
+    L = orc.lib()
+    cases = [(0, 0), (-1, 0xFFFFFFFF), ((1 << 31) - 1, 0xFFFFFFFF), (1 << 31, 0), (-(1 << 31) - 1, 0),
+             (1 << 40, (1 << 62) + 12345), (-(1 << 50), 1), ((1 << 62) - 7, (1 << 63) - 1), (-(1 << 62), 0)]
+    for _ in range(2000):
+        h = int(rng.integers(-(1 << 62), 1 << 62)) >> int(rng.integers(0, 62))
+        lo = int(rng.integers(0, 1 << 63)) >> int(rng.integers(0, 63))
+        cases.append((h, lo))
+    # exact ties: S = (2^24 + 1) * 2^k + 2^(k-1) rounds to even
+    for k in (40, 50, 60, 69):
+        s = ((1 << 24) + 1) * (1 << k) + (1 << (k - 1))
+        cases.append((s >> 32, s & 0xFFFFFFFF))
+    for h, lo in cases:
+        for e in (0, 47, 52):
+            got = np.float32(L.vo_fixed2_to_float(h, lo, e))
+            want = _f32_round(h * (1 << 32) + lo, e)
+            assert got == want, (h, lo, e, got, want)
+
+
+def test_gradient_sums_past_int64_oracle(orc):
+    """Three sites pulled one way by 2^20 targets: the fixed-point gradient
+    passes 2^63 in magnitude and still equals FP64 within 1e-6 (the
+    reference's float sums: about 1e-3)."""
+    from voromesh_gb300 import synth
+
+    gen = np.array([[0.2, 1.0], [1.0, 1.0], [1.0, 0.2]], np.float32)
+    tgt = (synth.uniform(23, 2, 1 << 20, -0.02, 0.02, shift=False) + np.float32([1.9, 1.0])).astype(np.float32)
+    f = orc.Fit(2.0, 2.0, 0.1, 12, 0.09, 1.0, 300, nthreads=8)
+    f.set_targets(tgt)
+    f.set_generators(gen, 3, 1, 2.0)
+    g, cnt, _ = f.gradient()
+    d = orc.Fit64(2.0, 2.0, float(np.float32(0.1)), 12, 0.09, 1.0, 300, nthreads=8)
+    d.set_targets(tgt)
+    d.set_generators(gen, 3, 1, 2.0)
+    g64, c64, _ = d.gradient()
+    assert cnt == c64 == len(tgt)
+    assert np.log2(np.abs(g64).max()) + orc.lib().vo_fixed_grad_exp(np.float32(0.1)) > 63.5
+    assert np.abs(g - g64).max() <= 1e-6 * np.abs(g64).max()

@@ -64,3 +64,38 @@ def test_noalloc_rejects_oversize(vm):
     assert lib.vm_build_grid_noalloc(C.c_void_p(8), 262145, 10, 10, 0.1, C.c_void_p(8), C.c_void_p(8),
                                      C.c_void_p(8), None) == 1
     assert lib.vm_build_grid_noalloc(None, 0, 1000, 1000, 0.1, C.c_void_p(8), None, None, None) == 1
+
+
+def test_noalloc_empty_and_side_stream(vm):
+    """n = 0 leaves every cell start at zero (after a call that filled them),
+    and a call enqueued on a side stream gives the same grid as one on the
+    legacy default stream."""
+    import torch
+
+    from voromesh_gb300 import synth
+    from voromesh_gb300._lib import check, load
+
+    lib = load()
+    n, gw, gh, spacing = 30000, 100, 100, 0.02
+    gen = torch.from_numpy(synth.uniform(31, 1, n)).cuda()
+    outs = []
+    side = torch.cuda.Stream()
+    for stream in (None, side):
+        d_start = torch.full((gw * gh + 1,), -7, dtype=torch.int32, device="cuda")
+        d_sidx = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+        d_spos = torch.full((n, 2), -7.0, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        handle = None if stream is None else C.c_void_p(stream.cuda_stream)
+        check(lib.vm_build_grid_noalloc(_dev_ptr(gen), n, gw, gh, spacing, _dev_ptr(d_start), _dev_ptr(d_sidx),
+                                        _dev_ptr(d_spos), handle), "vm_build_grid_noalloc")
+        torch.cuda.synchronize()
+        outs.append((d_start.cpu().numpy(), d_sidx.cpu().numpy(), d_spos.cpu().numpy()))
+    assert outs[0][0][-1] == n
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    d_start = torch.full((gw * gh + 1,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    check(lib.vm_build_grid_noalloc(None, 0, gw, gh, spacing, _dev_ptr(d_start), None, None, None),
+          "vm_build_grid_noalloc")
+    torch.cuda.synchronize()
+    assert not d_start.cpu().numpy().any()
