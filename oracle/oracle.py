@@ -47,11 +47,13 @@ def lib() -> C.CDLL:
         _lib.vo_fit_set_targets.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         _lib.vo_fit_set_generators.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float]
         _lib.vo_fit_begin_schedule.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        _lib.vo_fit_update_generators.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.vo_fit_get.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.vo_fit_grid.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.vo_fit_grid_size.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.vo_fit_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.vo_fit_iteration.argtypes = [C.c_void_p]
+        _lib.vo_fit_schedule_length.argtypes = [C.c_void_p]
         _lib.vo_fit64_create.restype = C.c_void_p
         _lib.vo_fit64_create.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
                                          C.c_double, C.c_void_p, C.c_int, C.c_uint, C.c_int]
@@ -228,8 +230,15 @@ class Fit:
         self.n = slotsW * slotsH
         lib().vo_fit_set_generators(self.h, P(g), slotsW, slotsH, slotCellSize)
 
+    def update_generators(self, g, cx0, cy0, cx1, cy1):
+        g = np.ascontiguousarray(g, np.float32)
+        lib().vo_fit_update_generators(self.h, P(g), cx0, cy0, cx1, cy1)
+
     def begin_schedule(self, it, cx0, cy0, cx1, cy1):
         lib().vo_fit_begin_schedule(self.h, it, cx0, cy0, cx1, cy1)
+
+    def schedule_length(self) -> int:
+        return lib().vo_fit_schedule_length(self.h)
 
     def step(self, k=1) -> float:
         return lib().vo_fit_step(self.h, k)

@@ -646,6 +646,20 @@ void vo_fit_set_generators(vo_fit *f, const vo_f2 *slots, int slotsW, int slotsH
     vo_fit_begin_schedule(f, f->paramIterations, 0, 0, f->slotsW, f->slotsH);
 }
 
+/* UpdateGenerators: voro_optimizer.cu:640-650 (the slots of the clamped
+ * rectangle are copied from the full slot array; nothing else changes) */
+void vo_fit_update_generators(vo_fit *f, const vo_f2 *slots, int cx0, int cy0, int cx1, int cy1)
+{
+    cx0 = cx0 > 0 ? cx0 : 0;
+    cy0 = cy0 > 0 ? cy0 : 0;
+    cx1 = cx1 < f->slotsW ? cx1 : f->slotsW;
+    cy1 = cy1 < f->slotsH ? cy1 : f->slotsH;
+    if (cx0 >= cx1 || cy0 >= cy1) return;
+    for (int y = cy0; y < cy1; ++y)
+        memcpy(f->gen + (size_t)y * f->slotsW + cx0, slots + (size_t)y * f->slotsW + cx0,
+               sizeof(vo_f2) * (size_t)(cx1 - cx0));
+}
+
 /* BeginSchedule: voro_optimizer.cu:652-687 */
 void vo_fit_begin_schedule(vo_fit *f, int iterations, int cx0, int cy0, int cx1, int cy1)
 {
@@ -738,6 +752,7 @@ float vo_fit_eval_loss(vo_fit *f)
 }
 
 int vo_fit_iteration(const vo_fit *f) { return f->iteration; }
+int vo_fit_schedule_length(const vo_fit *f) { return f->scheduleLength; }
 
 int vo_fit_grid_size(const vo_fit *f, int *gw, int *gh)
 {

@@ -123,11 +123,13 @@ vo_fit *vo_fit_create(float width, float height, float spacing, int K, float lrP
 void vo_fit_destroy(vo_fit *f);
 void vo_fit_set_targets(vo_fit *f, const vo_f2 *slots, int n);
 void vo_fit_set_generators(vo_fit *f, const vo_f2 *slots, int slotsW, int slotsH, float slotCellSize);
+void vo_fit_update_generators(vo_fit *f, const vo_f2 *slots, int cx0, int cy0, int cx1, int cy1);
 void vo_fit_begin_schedule(vo_fit *f, int iterations, int cx0, int cy0, int cx1, int cy1);
 /* Runs `steps` iterations; returns the last batch loss (loss / count). */
 float vo_fit_step(vo_fit *f, int steps);
 float vo_fit_eval_loss(vo_fit *f);
 int vo_fit_iteration(const vo_fit *f);
+int vo_fit_schedule_length(const vo_fit *f);
 int vo_fit_grid_size(const vo_fit *f, int *gw, int *gh);
 /* Copies out the generators (n float2) and, when non-NULL, m and v. */
 void vo_fit_get(const vo_fit *f, vo_f2 *gen, vo_f2 *m, vo_f2 *v);

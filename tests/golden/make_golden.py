@@ -44,15 +44,94 @@ def ref_grid(ref, gen, gw, gh, cell):
     return st, si, sp, gc
 
 
+def lround(x: float) -> int:
+    """std::lround: nearest integer, halves away from zero."""
+    return int(np.floor(x + 0.5)) if x >= 0 else -int(np.floor(-x + 0.5))
+
+
 def run_params(spacing, lr_ps, slots_w, slots_h, slot_cell, iterations, param_iterations, W=2.0, H=2.0,
-               gamma=0.5, ms=(80, 150, 200, 250)):
-    """RunParams of BeginSchedule(iterations) over the full slot rectangle (voro_optimizer.cu:658-675)."""
-    mss = [int(round(float(m) * iterations / param_iterations)) for m in ms]
+               gamma=0.5, ms=(80, 150, 200, 250), rect=None):
+    """RunParams of BeginSchedule(iterations, rect) (voro_optimizer.cu:658-675);
+    rect None = the full slot rectangle."""
+    cx0, cy0, cx1, cy1 = rect or (0, 0, slots_w, slots_h)
+    cx0, cy0, cx1, cy1 = max(cx0, 0), max(cy0, 0), min(cx1, slots_w), min(cy1, slots_h)
+    mss = [lround(float(m) * iterations / param_iterations) for m in ms]
     margin = f32(2.0) * f32(spacing)
-    rpf = np.array([f32(lr_ps) * f32(spacing), gamma, 0.9, 0.999, 1e-8, W, H, f32(0.0) - margin, f32(0.0) - margin,
-                    f32(slots_w) * f32(slot_cell) + margin, f32(slots_h) * f32(slot_cell) + margin], np.float32)
-    rpi = np.array(mss + [slots_w, 0, 0, slots_w, slots_h], np.int32)
+    sc = f32(slot_cell)
+    rpf = np.array([f32(lr_ps) * f32(spacing), gamma, 0.9, 0.999, 1e-8, W, H, f32(cx0) * sc - margin,
+                    f32(cy0) * sc - margin, f32(cx1) * sc + margin, f32(cy1) * sc + margin], np.float32)
+    rpi = np.array(mss + [slots_w, cx0, cy0, cx1, cy1], np.int32)
     return rpf, rpi
+
+
+class RefFit:
+    """The reference's host sequence (voro_optimizer.cu:613-744) driven over its
+    own kernels: SetGenerators, UpdateGenerators, BeginSchedule with a slot
+    rectangle (moments of the rectangle zeroed, step counter reset) and Step
+    (beginIteration, grid build, vorolossKernel, adamKernel)."""
+
+    def __init__(self, ref, gen, slots_w, slots_h, slot_cell, targets, K, spacing, lr_ps, fraction,
+                 param_iterations, seed=1):
+        self.ref, self.K, self.spacing, self.lr_ps = ref, K, float(f32(spacing)), lr_ps
+        self.fraction, self.seed, self.param_iterations = fraction, seed, param_iterations
+        self.w, self.h, self.slot_cell = slots_w, slots_h, slot_cell
+        self.gen = np.ascontiguousarray(gen, np.float32).copy()
+        self.m = np.zeros_like(self.gen)
+        self.v = np.zeros_like(self.gen)
+        self.grad = np.zeros_like(self.gen)
+        self.targets = np.ascontiguousarray(targets, np.float32)
+        self.st = np.zeros(2, np.int32)
+        self.gw, self.gh = orc.grid_dims(2.0, 2.0, self.spacing)
+        self.begin_schedule(param_iterations)
+
+    def begin_schedule(self, iterations, rect=None):
+        self.rpf, self.rpi = run_params(self.spacing, self.lr_ps, self.w, self.h, self.slot_cell, iterations,
+                                        self.param_iterations, rect=rect)
+        cx0, cy0, cx1, cy1 = (int(v) for v in self.rpi[5:9])
+        if cx0 < cx1 and cy0 < cy1:
+            for a in (self.m, self.v):
+                a.reshape(self.h, self.w, 2)[cy0:cy1, cx0:cx1] = 0.0
+        self.st[:] = 0
+        self.length, self.iteration = iterations, 0
+
+    def update_generators(self, slots, rect):
+        cx0, cy0, cx1, cy1 = max(rect[0], 0), max(rect[1], 0), min(rect[2], self.w), min(rect[3], self.h)
+        if cx0 < cx1 and cy0 < cy1:
+            s = np.ascontiguousarray(slots, np.float32).reshape(self.h, self.w, 2)
+            self.gen.reshape(self.h, self.w, 2)[cy0:cy1, cx0:cx1] = s[cy0:cy1, cx0:cx1]
+
+    def step(self, k):
+        losses = []
+        n = len(self.gen)
+        sl = np.zeros(1, np.float32)
+        for _ in range(k):
+            self.st[0] += 1
+            self.st[1] = 0
+            sl[0] = 0
+            g = ref_grid(self.ref, self.gen, self.gw, self.gh, self.spacing)
+            self.ref.ref_loss(self.K, P(self.targets), len(self.targets), P(g[0]), P(g[1]), P(g[2]), self.gw,
+                              self.gh, C.c_float(self.spacing), P(self.gen), P(self.grad), P(self.st), P(sl),
+                              P(self.rpf), P(self.rpi), C.c_float(self.fraction), C.c_uint(self.seed))
+            losses.append(sl[0] / self.st[1] if self.st[1] else f32(0))
+            self.ref.ref_adam(P(self.gen), P(self.m), P(self.v), P(self.grad), n, int(self.st[0]), int(self.st[1]),
+                              P(self.rpf), P(self.rpi))
+        self.iteration = int(self.st[0])
+        return np.array(losses, np.float32)
+
+
+def ref_local_edit(ref, case):
+    """The local-edit case (tests/edit_case.py) through RefFit: the global
+    schedule, then the edit and the local schedule. Returns the state after
+    each phase."""
+    f = RefFit(ref, case.generators, case.slots, case.slots, case.slot_cell, case.targets, case.K, case.spacing,
+               case.lr_per_spacing, case.fraction, case.iterations)
+    l1 = f.step(case.global_steps)
+    mid = (f.gen.copy(), f.m.copy(), f.v.copy(), l1)
+    f.targets = np.ascontiguousarray(case.targets2, np.float32)
+    f.update_generators(case.slots2, case.rect)
+    f.begin_schedule(case.local_iterations, case.rect)
+    l2 = f.step(f.length - f.iteration)
+    return mid, (f.gen.copy(), f.m.copy(), f.v.copy(), l2)
 
 
 def ref_fit(ref, gen0, tg, K, spacing, lr_ps, frac, steps, seed=1, param_iterations=300):
@@ -108,6 +187,14 @@ def main():
         g, m, v, losses = ref_fit(ref, gen, tg, 12, 0.05, spec.lrPerSpacing, frac, steps)
         key = f"plain_f{int(frac * 100)}"
         out.update({f"{key}_gen": g, f"{key}_m": m, f"{key}_v": v, f"{key}_losses": losses})
+    # ---- the local-edit sequence: global schedule, then UpdateTargets, UpdateGenerators(rect),
+    #      BeginSchedule(localIterations, rect) and Optimize (tests/edit_case.py)
+    sys.path.insert(0, str(HERE.parent))
+    from edit_case import edit_case  # noqa: E402
+
+    (g1, m1, v1, l1), (g2, m2, v2, l2) = ref_local_edit(ref, edit_case())
+    out.update(edit_global_gen=g1, edit_global_m=m1, edit_global_v=v1, edit_global_losses=l1, edit_local_gen=g2,
+               edit_local_m=m2, edit_local_v=v2, edit_local_losses=l2)
     # ---- k=16 loss pass (kLossK patched to 16)
     gen16 = synth.uniform(3, 1, 1024)
     tg16 = synth.circle(3, 2, 8192, 0.6, 1e-3)

@@ -412,3 +412,44 @@ def test_gradient_sums_past_int64_oracle(orc):
     assert cnt == c64 == len(tgt)
     assert np.log2(np.abs(g64).max()) + orc.lib().vo_fixed_grad_exp(np.float32(0.1)) > 63.5
     assert np.abs(g - g64).max() <= 1e-6 * np.abs(g64).max()
+
+
+def _edit_case():
+    import sys
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from edit_case import edit_case, run_oracle
+
+    return edit_case(), run_oracle
+
+
+def test_local_edit_schedule(orc, gold):
+    """The editor's local edit (global schedule, UpdateTargets,
+    UpdateGenerators and BeginSchedule over a slot rectangle, Optimize) on the
+    oracle in reference mode against the reference kernels' fixture: every
+    loss, position and moment after each phase."""
+    case, run_oracle = _edit_case()
+    (g1, m1, v1, l1), (g2, m2, v2, l2), _ = run_oracle(orc, case, orc.ACC_REF, orc.POW_REF)
+    assert np.array_equal(l1, gold["edit_global_losses"]) and np.array_equal(l2, gold["edit_local_losses"])
+    assert np.array_equal(g1, gold["edit_global_gen"]) and np.array_equal(g2, gold["edit_local_gen"])
+    assert np.array_equal(m1, gold["edit_global_m"]) and np.array_equal(v1, gold["edit_global_v"])
+    assert np.array_equal(m2, gold["edit_local_m"]) and np.array_equal(v2, gold["edit_local_v"])
+    # slots outside the rectangle are frozen through the local schedule
+    cx0, cy0, cx1, cy1 = case.rect
+    frozen = np.ones((case.slots, case.slots), bool)
+    frozen[cy0:cy1, cx0:cx1] = False
+    frozen = frozen.reshape(-1)
+    assert np.array_equal(g2[frozen], g1[frozen]) and not np.array_equal(g2[~frozen], g1[~frozen])
+
+
+def test_local_edit_matches_live_reference(orc):
+    """The same sequence against the reference kernels run live here."""
+    if not orc.ref_available():
+        pytest.skip("the reference kernels are not compiled here")
+    mg = _make_golden_module()
+    case, run_oracle = _edit_case()
+    (rg1, rm1, rv1, rl1), (rg2, rm2, rv2, rl2) = mg.ref_local_edit(orc.ref(), case)
+    (g1, m1, v1, l1), (g2, m2, v2, l2), _ = run_oracle(orc, case, orc.ACC_REF, orc.POW_REF)
+    assert np.array_equal(l1, rl1) and np.array_equal(l2, rl2)
+    assert np.array_equal(g1, rg1) and np.array_equal(m1, rm1) and np.array_equal(v1, rv1)
+    assert np.array_equal(g2, rg2) and np.array_equal(m2, rm2) and np.array_equal(v2, rv2)
