@@ -124,6 +124,7 @@ struct vmb_batch {
     int lossVariant = 1, lossTile = 256, lossGrid = 0;
     bool dirty = true;
     std::vector<VmState> hostStates;
+    DevBuf<int> block5Buf; // a fit's largest 5x5-block target count, read back at vmb_add_fit
 };
 
 namespace {
@@ -469,8 +470,15 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
         release_fit(b, f);
         return rc;
     }
-    int live = 0;
-    if ((e = cudaMemcpyAsync(&live, liveAt, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
+    int live = 0, b5 = 0;
+    if ((rc = b->block5Buf.reserve(1))) {
+        releaseTmp();
+        release_fit(b, f);
+        return rc;
+    }
+    if ((e = vm_launch_block5_max(f.tset.start, f.gridW, f.gridH, f.tset.sub, b->block5Buf.p, b->stream)) ||
+        (e = cudaMemcpyAsync(&live, liveAt, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
+        (e = cudaMemcpyAsync(&b5, b->block5Buf.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
         (e = cudaStreamSynchronize(b->stream))) {
         releaseTmp();
         release_fit(b, f);
@@ -479,6 +487,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     releaseTmp();
     f.liveTargets = live;
     D.nTargets = live;
+    D.fastLimit = vm_fast_limit(b5, D.gradExp);
     if ((rc = single_set_build(b, f.sites, 1, 1))) { // the grid of the initial generators
         release_fit(b, f);
         return rc;

@@ -54,17 +54,11 @@ __device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) 
 
 // round-half-even(v * 2^e) as int64, saturating at +-2^62, NaN -> 0; integer
 // operations only (64-bit float->int conversions run on the narrow FP64 pipe).
-// A saturated term (|v| 2^e >= 2^62: near-coincident sites) is counted in
-// *clamped when that pointer is given.
-static __device__ __noinline__ long long fx_from_float_any(float v, int e, int *clamped)
+static __device__ __noinline__ long long fx_from_float_any(float v, int e)
 {
     unsigned u = __float_as_uint(v);
     int ex = (int)((u >> 23) & 0xFFu);
-    if (ex == 0xFF) {
-        if (u & 0x7FFFFFu) return 0;
-        if (clamped) atomicAdd(clamped, 1);
-        return (u >> 31) ? -4611686018427387904LL : 4611686018427387904LL;
-    }
+    if (ex == 0xFF) return (u & 0x7FFFFFu) ? 0 : ((u >> 31) ? -4611686018427387904LL : 4611686018427387904LL);
     unsigned m = u & 0x7FFFFFu;
     int k; // |v| 2^e = m 2^k
     if (ex == 0) { // subnormal v
@@ -76,7 +70,6 @@ static __device__ __noinline__ long long fx_from_float_any(float v, int e, int *
     }
     long long mag;
     if (k >= 0) {
-        if (k > 38 && clamped) atomicAdd(clamped, 1);
         mag = k > 38 ? 4611686018427387904LL : ((long long)m << k);
     } else if (k < -24) {
         mag = 0;
@@ -93,7 +86,7 @@ static __device__ __noinline__ long long fx_from_float_any(float v, int e, int *
 
 // The same with the common case inline: a normal v whose scaled value is an
 // integer below 2^62 (a plain shift of the significand, no rounding).
-__device__ __forceinline__ long long fx_from_float(float v, int e, int *clamped = nullptr)
+__device__ __forceinline__ long long fx_from_float(float v, int e)
 {
     unsigned u = __float_as_uint(v);
     int ex = (int)((u >> 23) & 0xFFu);
@@ -102,20 +95,32 @@ __device__ __forceinline__ long long fx_from_float(float v, int e, int *clamped 
         long long mag = (long long)((u & 0x7FFFFFu) | 0x800000u) << k;
         return (u >> 31) ? -mag : mag;
     }
-    return fx_from_float_any(v, e, clamped);
+    return fx_from_float_any(v, e);
 }
 
 __device__ __forceinline__ float fx_to_float(long long v, int e) { return __ll2float_rn(v) * pow2f(-e); }
 
 // ---- exact per-site gradient sums ----------------------------------------------
-// A site's gradient component is the exact integer sum S of int64
-// contributions x (|x| < 2^63). Each x is split as x = hi * 2^32 + lo with
-// lo = x mod 2^32 in [0, 2^32) and hi = x >> 32 (arithmetic), and the site
-// keeps L = sum(lo) (unsigned) and H = sum(hi) (signed) in two 64-bit words.
-// A site receives fewer than 2^31 contributions (one per target at most), so
-// L < 2^63 and |H| < 2^62: neither word wraps and S = H * 2^32 + L exactly,
-// for any input, where one 64-bit sum would wrap past 2^63. Per slot the
-// words are laid out as {Lx, Ly, Hx, Hy} (kGradWords per slot).
+// A site's gradient component is the exact integer sum S of its fixed-point
+// terms (each at most 2^62 in magnitude). gradX holds three sections of
+// 64-bit words per slot, (x, y) each:
+//
+//   L       the loss kernel's fast path: one 64-bit sum, exact modulo 2^64.
+//           The fast path gives a target only sites of the 5x5 cell block
+//           around its own cell, so a site receives at most T5 terms (T5: the
+//           most live targets in any 5x5 block) and |S| <= T5 * max|term|.
+//           Every term is compared with the fit's fastLimit, 2^62 / (T5 2^e)
+//           rounded down (vm_fast_limit): below it no site sum can leave the
+//           int64 range, so L holds S itself. A warp that meets a term at or
+//           above it flags the fit, and the fit's whole gradient is
+//           recomputed into DL/DH instead (k_loss_exact), with L ignored.
+//   DL, DH  the deferred (ring-search) targets and flagged fits, in the
+//           unconditional split x = hi * 2^32 + lo, lo in [0, 2^32): a site
+//           receives fewer than 2^31 terms, so neither word wraps.
+//
+// So every site sum is exact for any input, and the fast path costs one
+// 64-bit reduction per component and one comparison per target. At the
+// 1M-site workload T5 * max|term| is about 2^54.6, far below 2^62.
 
 __host__ __device__ __forceinline__ float vm_pow2f(int e)
 {
@@ -144,20 +149,16 @@ __host__ __device__ __forceinline__ float vm_s64_to_float(long long v)
 #endif
 }
 
-// S * 2^-e rounded once to float when |S| >= 2^63 (T = S >> 32 outside the
-// int32 range, low = S mod 2^32): the 128-bit magnitude is shifted so its
-// leading one is bit 63 of a 64-bit word, the bits shifted out are folded
-// into bit 0 as a sticky bit (far below the rounding position), and the word
-// is converted with round-to-nearest-even and scaled back by a power of two.
-__host__ __device__ __noinline__ inline float fx2_to_float_wide(long long T, unsigned long long low, int e)
+// v * 2^-e rounded once to float, v a 128-bit integer: the magnitude is
+// shifted so its leading one is bit 63 of a 64-bit word, the bits shifted
+// out are folded into bit 0 as a sticky bit (far below the rounding
+// position), and the word is converted with round-to-nearest-even and scaled
+// back by powers of two (exact).
+__host__ __device__ __noinline__ inline float i128_to_float(__int128 v, int e)
 {
-    unsigned long long lo = ((unsigned long long)T << 32) | low;
-    unsigned long long hi = (unsigned long long)(T >> 32);
-    bool neg = T < 0;
-    if (neg) {
-        lo = ~lo + 1ull;
-        hi = ~hi + (lo == 0 ? 1ull : 0ull);
-    }
+    bool neg = v < 0;
+    unsigned __int128 m = neg ? (unsigned __int128)0 - (unsigned __int128)v : (unsigned __int128)v;
+    unsigned long long hi = (unsigned long long)(m >> 64), lo = (unsigned long long)m;
     float f;
     if (hi == 0) {
         f = vm_u64_to_float(lo);
@@ -167,8 +168,7 @@ __host__ __device__ __noinline__ inline float fx2_to_float_wide(long long T, uns
 #else
         int c = __builtin_clzll(hi);
 #endif
-        // |S| < 2^95, so hi < 2^31 and c is in [33, 63]
-        unsigned long long top = (hi << c) | (lo >> (64 - c));
+        unsigned long long top = c ? (hi << c) | (lo >> (64 - c)) : hi;
         unsigned long long rest = lo << c;
         top |= rest != 0 ? 1ull : 0ull;
         f = vm_u64_to_float(top) * vm_pow2f(64 - c);
@@ -177,38 +177,29 @@ __host__ __device__ __noinline__ inline float fx2_to_float_wide(long long T, uns
     return f * vm_pow2f(-e);
 }
 
-// S * 2^-e, S = H * 2^32 + L, rounded once to float (the same value as
-// converting S exactly and scaling, which is what (float)S * 2^-e gives when
-// S fits an int64).
-__host__ __device__ __forceinline__ float fx2_to_float(long long H, unsigned long long L, int e)
+// The site sum of one component, rounded once to float and scaled by 2^-e:
+// L (when useL) plus DH * 2^32 + DL.
+__host__ __device__ __noinline__ inline float fx_site_to_float(long long L, bool useL, unsigned long long DL,
+                                                               long long DH, int e)
 {
-    long long T = H + (long long)(L >> 32); // S = T * 2^32 + (L mod 2^32)
-    unsigned long long low = L & 0xFFFFFFFFull;
-    if (T >= -2147483648LL && T <= 2147483647LL)
-        return vm_s64_to_float((long long)(((unsigned long long)T << 32) | low)) * vm_pow2f(-e);
-    return fx2_to_float_wide(T, low, e);
+    __int128 v = (useL ? (__int128)L : (__int128)0) + (__int128)DH * ((__int128)1 << 32) + (__int128)DL;
+    return i128_to_float(v, e);
 }
 
-// Adds contributions x, y to the split words of site s (G: kGradWords per slot).
-__device__ __forceinline__ void fx2_red(unsigned long long *G, int s, long long x, long long y)
+// Adds a contribution (x, y) to site s in the unconditional split words
+// (sections DL and DH of G, n slots).
+static __device__ __noinline__ void fxd_red(unsigned long long *G, int n, int s, long long x, long long y, int *dUsed)
 {
-    unsigned long long *g = G + (size_t)kGradWords * s;
+    unsigned long long *DL = G + 2 * (size_t)n + 2 * (size_t)s, *DH = DL + 2 * (size_t)n;
     if (x) {
-        atomicAdd(&g[0], (unsigned long long)x & 0xFFFFFFFFull);
-        long long h = x >> 32;
-        if (h) atomicAdd(&g[2], (unsigned long long)h);
+        atomicAdd(&DL[0], (unsigned long long)x & 0xFFFFFFFFull);
+        if (x >> 32) atomicAdd(&DH[0], (unsigned long long)(x >> 32));
     }
     if (y) {
-        atomicAdd(&g[1], (unsigned long long)y & 0xFFFFFFFFull);
-        long long h = y >> 32;
-        if (h) atomicAdd(&g[3], (unsigned long long)h);
+        atomicAdd(&DL[1], (unsigned long long)y & 0xFFFFFFFFull);
+        if (y >> 32) atomicAdd(&DH[1], (unsigned long long)(y >> 32));
     }
-}
-
-// |v| < 2^62: a further term (|x| <= 2^62) can be added without overflow.
-__device__ __forceinline__ bool fx_small(long long v)
-{
-    return (unsigned)((int)(v >> 32) + 0x40000000) < 0x80000000u;
+    atomicOr(dUsed, 1);
 }
 
 __device__ __forceinline__ void fxl_from_float(float v, int e, unsigned long long &lo, unsigned long long &hi)
@@ -311,10 +302,16 @@ __device__ __forceinline__ void adam_schedule(const VmFit &F)
 // to this queue and resolved by k_loss_exact in dense warps, so one hard
 // target does not stall the 31 other lanes of its warp on the long ring
 // search. The queue holds every live target, so it cannot overflow.
+// The same header lists the fits whose fast-path gradient bound failed in
+// the current pass (see the exact per-site sums above); k_loss_exact
+// recomputes their gradients.
+constexpr int kMaxFlagged = 256;
 struct SlowQueue {
     int count;
     int capacity;
     int2 *items; // (fit, local target index)
+    int nFlagged;
+    int flagged[kMaxFlagged];
 };
 
 } // namespace vmk

@@ -525,10 +525,10 @@ __device__ __forceinline__ void load_fit(const VmFit *__restrict__ fits, int f, 
 
 // A lane's running gradient sum for one site: consecutive targets of a lane
 // mostly share their nearest site and bisector neighbour, so the sum reaches
-// the fit's split accumulators only when the site changes (integer sums, so
-// the grouping does not change the result). A running sum is also flushed
-// before it could overflow: terms are at most 2^62 in magnitude, so a sum
-// below 2^62 takes one more term safely.
+// the fit's accumulators (section L of gradX) only when the site changes: one
+// 64-bit reduction per component (integer sums modulo 2^64, so neither the
+// grouping nor an intermediate wrap changes the result; the block bound
+// below keeps the sums themselves in range).
 struct RunSum {
     int site = -1;
     long long x = 0, y = 0;
@@ -536,19 +536,34 @@ struct RunSum {
 
 __device__ __forceinline__ void run_flush(RunSum &r, unsigned long long *G)
 {
-    if (r.site >= 0) fx2_red(G, r.site, r.x, r.y);
+    if (r.site >= 0) {
+        if (r.x) atomicAdd(&G[2 * (size_t)r.site], (unsigned long long)r.x);
+        if (r.y) atomicAdd(&G[2 * (size_t)r.site + 1], (unsigned long long)r.y);
+    }
     r.site = -1;
     r.x = r.y = 0;
 }
 
 __device__ __forceinline__ void run_add(RunSum &r, int site, long long x, long long y, unsigned long long *G)
 {
-    if (site != r.site || !fx_small(r.x) || !fx_small(r.y)) {
+    if (site != r.site) {
         run_flush(r, G);
         r.site = site;
     }
     r.x += x;
     r.y += y;
+}
+
+// A warp whose lanes met a gradient term at or above the fit's fastLimit
+// (every term below it keeps every site sum below 2^62) flags the fit, once,
+// for the exact recomputation.
+__device__ __forceinline__ void flag_fit(const VmFit &F, int f, SlowQueue *queue)
+{
+    if (atomicExch(&F.state->needExact, 1) == 0) {
+        int k = atomicAdd(&queue->nFlagged, 1);
+        if (k < kMaxFlagged) queue->flagged[k] = f;
+        else atomicOr(&F.state->errors, VM_KERR_CAPACITY);
+    }
 }
 
 // One block takes a contiguous range of tiles (THREADS targets each) of the
@@ -594,6 +609,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         int aCnt = 0, aSlow = 0;
         unsigned long long *G = reinterpret_cast<unsigned long long *>(F.gradX);
         RunSum run0, runJ;
+        bool overLimit = false; // this lane met a gradient term at or above F.fastLimit
         for (int base = w0; base < w1; base += 32) {
             int local = base + lane;
             bool valid = local < w1;
@@ -682,14 +698,17 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 aCnt += 1;
                 if (mode == 0) {
                     int e = F.gradExp;
-                    int *cl = &F.state->clamped;
-                    run_add(run0, o.i0, fx_from_float(o.g0x, e, cl), fx_from_float(o.g0y, e, cl), G);
-                    run_add(runJ, o.j, fx_from_float(o.gjx, e, cl), fx_from_float(o.gjy, e, cl), G);
+                    run_add(run0, o.i0, fx_from_float(o.g0x, e), fx_from_float(o.g0y, e), G);
+                    run_add(runJ, o.j, fx_from_float(o.gjx, e), fx_from_float(o.gjy, e), G);
+                    // (an infinite term is over; a NaN term converts to 0 and compares false)
+                    overLimit |= fmaxf(fmaxf(fabsf(o.g0x), fabsf(o.g0y)), fmaxf(fabsf(o.gjx), fabsf(o.gjy))) >=
+                                 F.fastLimit;
                 }
             }
         }
         run_flush(run0, G);
         run_flush(runJ, G);
+        if (__any_sync(kFull, overLimit) && lane == 0) flag_fit(F, f, queue);
         // the loss, count and fallbacks of this fit: warp, block, then one atomic each
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
@@ -725,16 +744,19 @@ __global__ void __launch_bounds__(THREADS, MINB)
 }
 
 // The deferred targets: exact ring search, one target per thread, with the
-// loss, count and gradient added straight into the fit's accumulators. In a
-// step pass it also writes each fit's Adam schedule for the step.
+// loss and count added straight into the fit's accumulators and the gradient
+// into its exact split words. In a step pass it also writes each fit's Adam
+// schedule for the step, and recomputes the whole gradient of every fit whose
+// fast-path bound failed (its deferred targets are then part of that).
 __global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fits, int nFits, int mode,
                                                     SlowQueue *queue)
 {
+    int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     if (mode == 0)
-        for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nFits; f += gridDim.x * blockDim.x)
+        for (int f = tid; f < nFits; f += stride)
             if (fits[f].active) adam_schedule(fits[f]); // for the Adam kernel that follows
     int n = min(queue->count, queue->capacity);
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    for (int q = tid; q < n; q += stride) {
         int2 it = queue->items[q];
         const VmFit &F = fits[it.x];
         float2 p = F.tpos[it.y];
@@ -750,12 +772,28 @@ __global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fi
         fxl_from_float(o.loss, F.lossExp, lo, hi);
         atomic_add128(&F.state->accLo, &F.state->accHi, lo, hi);
         atomicAdd(&F.state->accCount, 1);
-        if (mode == 0) {
+        if (mode == 0 && !F.state->needExact) {
             int e = F.gradExp;
-            int *cl = &F.state->clamped;
             unsigned long long *g = reinterpret_cast<unsigned long long *>(F.gradX);
-            fx2_red(g, o.j, fx_from_float(o.gjx, e, cl), fx_from_float(o.gjy, e, cl));
-            fx2_red(g, o.i0, fx_from_float(o.g0x, e, cl), fx_from_float(o.g0y, e, cl));
+            fxd_red(g, F.nSlots, o.j, fx_from_float(o.gjx, e), fx_from_float(o.gjy, e), &F.state->dUsed);
+            fxd_red(g, F.nSlots, o.i0, fx_from_float(o.g0x, e), fx_from_float(o.g0y, e), &F.state->dUsed);
+        }
+    }
+    if (mode != 0) return;
+    int nf = min(queue->nFlagged, kMaxFlagged);
+    for (int k = 0; k < nf; ++k) {
+        const VmFit &F = fits[queue->flagged[k]];
+        unsigned iter = (unsigned)(F.state->iter + 1);
+        unsigned long long *g = reinterpret_cast<unsigned long long *>(F.gradX);
+        int e = F.gradExp;
+        for (int t = tid; t < F.nTargets; t += stride) {
+            float2 p = F.tpos[t];
+            bool take = p.x >= F.bx0 && p.x <= F.bx1 && p.y >= F.by0 && p.y <= F.by1;
+            if (take && F.fraction < 1.0f) take = rand01((unsigned)F.tslot[t], iter, F.seed) < F.fraction;
+            TgtOut o;
+            if (!take || !loss_exact(F, p, o)) continue;
+            fxd_red(g, F.nSlots, o.j, fx_from_float(o.gjx, e), fx_from_float(o.gjy, e), &F.state->dUsed);
+            fxd_red(g, F.nSlots, o.i0, fx_from_float(o.g0x, e), fx_from_float(o.g0y, e), &F.state->dUsed);
         }
     }
 }

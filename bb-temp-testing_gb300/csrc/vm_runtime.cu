@@ -133,7 +133,8 @@ struct vm_optimizer {
     VmFit fit{};
     MeshHost mesh;
     long long exactTotal = 0;
-    long long clampedTotal = 0; // gradient terms clamped to +-2^62 in fixed point
+    int block5Max = 0;          // most live targets in any 5x5 block of cells (sets the split shift)
+    DevBuf<int> block5Buf;
 
     int numSlots() const { return slotsW * slotsH; }
 };
@@ -160,6 +161,7 @@ int upload_tables(vm_optimizer *h)
     F.lossExp = 64 - 2 * floor_log2f(h->spacing);
     F.nTargets = h->liveTargets;
     F.active = 1;
+    F.fastLimit = vm_fast_limit(h->block5Max, F.gradExp);
     F.gen = h->gen.p; F.m = h->m.p; F.v = h->v.p; F.gradX = h->gradX.p;
     F.key = h->key.p; F.rank = h->rank.p; F.counts = h->counts.p; F.start = h->start.p; F.tileSums = h->tileSums.p;
     F.sortedIdx = h->sortedIdx.p; F.sortedPos = h->sortedPos.p;
@@ -396,8 +398,12 @@ int sort_targets(vm_optimizer *h)
     if ((e = vm_launch_scan(h->dTargets.p, h->dTPre.p + 2, 1, keyTiles, h->stream))) return cuda_fail(e, "target scan");
     if ((e = vm_launch_scatter(h->dTargets.p, h->dTPre.p, 1, tb, nullptr, h->stream)))
         return cuda_fail(e, "target scatter");
-    int live = 0;
-    if ((e = cudaMemcpyAsync(&live, h->tstart.p + keys, sizeof(int), cudaMemcpyDeviceToHost, h->stream)))
+    int live = 0, b5 = 0;
+    if ((rc = h->block5Buf.reserve(1))) return rc;
+    if ((e = vm_launch_block5_max(h->tstart.p, h->gridW, h->gridH, sub, h->block5Buf.p, h->stream)))
+        return cuda_fail(e, "target block counts");
+    if ((e = cudaMemcpyAsync(&live, h->tstart.p + keys, sizeof(int), cudaMemcpyDeviceToHost, h->stream)) ||
+        (e = cudaMemcpyAsync(&b5, h->block5Buf.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream)))
         return cuda_fail(e, "live targets");
     // the tables above live on the host stack
     if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "target sort");
@@ -406,6 +412,7 @@ int sort_targets(vm_optimizer *h)
     h->ttileSums.release();
     if (live != h->liveTargets) drop_graph(h);
     h->liveTargets = live;
+    h->block5Max = b5;
     int qcap = std::max(live, 1); // every live target fits: the loss never overflows the queue
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -743,7 +750,6 @@ int vm_step(vm_optimizer *h, int iterations, float *gpuMs)
     h->iteration = st.iter;
     h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
     h->exactTotal = st.slowTotal;
-    h->clampedTotal = st.clamped;
     float ms = 0.0f;
     if ((e = cudaEventElapsedTime(&ms, h->ev0, h->ev1))) return cuda_fail(e, "elapsed");
     if (gpuMs) *gpuMs = ms;
@@ -786,7 +792,6 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
     h->iteration = st.iter;
     h->lastBatchLoss = st.count > 0 ? st.loss / (float)st.count : 0.0f;
     h->exactTotal = st.slowTotal;
-    h->clampedTotal = st.clamped;
     for (int k = 0; k < iterations; ++k) {
         cudaEvent_t *ev = &h->timing[(size_t)k * 5];
         for (int j = 0; j < 4; ++j) {
@@ -849,7 +854,6 @@ int vm_info(vm_optimizer *h, vm_info_t *out)
     out->gridH = h->gridH;
     out->lastBatchLoss = h->lastBatchLoss;
     out->exactTargets = h->exactTotal;
-    out->clampedTerms = h->clampedTotal;
     return VM_OK;
 }
 
@@ -963,6 +967,8 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
     if ((e = cudaMemsetAsync(h->gradX.p, 0, sizeof(long long) * kGradWords * (size_t)n, h->stream)))
         return cuda_fail(e, "probe clear");
     if ((rc = read_state(h, st))) return rc;
+    // the pass's gradient flags were read above; clear them with the words
+    if ((e = cudaMemsetAsync(&h->state.p->needExact, 0, 2 * sizeof(int), h->stream))) return cuda_fail(e, "probe flags");
     h->fit = saved;
     if ((rc = upload_tables(h))) return rc;
     int cap = h->targetCapacity;
@@ -977,11 +983,10 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
         if (loss) loss[s] = hl[t];
     }
     if (grad) {
-        for (size_t k = 0; k < (size_t)n; ++k) {
-            const long long *w = &g[kGradWords * k]; // {Lx, Ly, Hx, Hy}
-            grad[2 * k] = vmk::fx2_to_float(w[2], (unsigned long long)w[0], h->fit.gradExp);
-            grad[2 * k + 1] = vmk::fx2_to_float(w[3], (unsigned long long)w[1], h->fit.gradExp);
-        }
+        // sections L, DL, DH of 2 words per slot; L is void when the pass redid the gradient exactly
+        const long long *L = g.data(), *DL = L + 2 * (size_t)n, *DH = DL + 2 * (size_t)n;
+        for (size_t k = 0; k < 2 * (size_t)n; ++k)
+            grad[k] = vmk::fx_site_to_float(L[k], !st.needExact, (unsigned long long)DL[k], DH[k], h->fit.gradExp);
     }
     if (count) *count = st.count;
     if (lossSum) *lossSum = st.loss;

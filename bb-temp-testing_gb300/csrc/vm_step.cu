@@ -72,6 +72,8 @@ __global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ 
         st->accLo = 0;
         st->accHi = 0;
         st->accCount = 0;
+        st->needExact = 0;
+        st->dUsed = 0;
     }
     grid_scatter_one(sets[f], local * blockDim.x + threadIdx.x);
 }
@@ -80,7 +82,10 @@ __global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ 
 __global__ void k_finalize(const VmFit *__restrict__ fits, int nFits, SlowQueue *queue)
 {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f == 0) queue->count = 0;
+    if (f == 0) {
+        queue->count = 0;
+        queue->nFlagged = 0;
+    }
     if (f >= nFits) return;
     VmState *st = fits[f].state;
     st->loss = fxl_to_float(st->accLo, st->accHi, fits[f].lossExp);
@@ -97,7 +102,10 @@ __global__ void k_finalize(const VmFit *__restrict__ fits, int nFits, SlowQueue 
 __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits, const int *__restrict__ prefix,
                                                   int nFits, SlowQueue *queue)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) queue->count = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        queue->count = 0;
+        queue->nFlagged = 0;
+    }
     int f = find_fit(prefix, nFits, blockIdx.x);
     const VmFit &F = fits[f];
     if (!F.active) return;
@@ -108,11 +116,26 @@ __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits
     float lr = st->schedLr, bc1 = st->schedBc1, bc2 = st->schedBc2;
     int count = st->accCount;
     float scale = 1.0f / (float)(count > 1 ? count : 1);
-    // the exact split sums {Lx, Ly} {Hx, Hy} of this slot, cleared for the next step
-    longlong2 *gw = reinterpret_cast<longlong2 *>(F.gradX) + 2 * (size_t)i;
-    longlong2 gl = gw[0], gh = gw[1];
+    // this slot's gradient: section L of gradX (one 64-bit sum per component)
+    // or, when the pass used the exact split words (deferred targets, or a
+    // fit whose fast-path bound failed), the exact sum of all three sections;
+    // the words are cleared for the next step
+    longlong2 *gw = reinterpret_cast<longlong2 *>(F.gradX) + i;
+    longlong2 gl = gw[0];
     if (gl.x | gl.y) gw[0] = make_longlong2(0, 0);
-    if (gh.x | gh.y) gw[1] = make_longlong2(0, 0);
+    float grx, gry;
+    if ((st->dUsed | st->needExact) == 0) {
+        grx = scale * fx_to_float(gl.x, F.gradExp);
+        gry = scale * fx_to_float(gl.y, F.gradExp);
+    } else {
+        size_t sec = (size_t)F.nSlots;
+        bool useL = !st->needExact;
+        longlong2 gdl = gw[sec], gdh = gw[2 * sec];
+        gw[sec] = make_longlong2(0, 0);
+        gw[2 * sec] = make_longlong2(0, 0);
+        grx = scale * fx_site_to_float(gl.x, useL, (unsigned long long)gdl.x, gdh.x, F.gradExp);
+        gry = scale * fx_site_to_float(gl.y, useL, (unsigned long long)gdl.y, gdh.y, F.gradExp);
+    }
     float2 p = F.gen[i];
     bool inRegion = true;
     if (F.cx0 != 0 || F.cy0 != 0 || F.cx1 != F.slotsW || F.cy1 != F.slotsH) {
@@ -120,8 +143,6 @@ __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits
         inRegion = sx >= F.cx0 && sx < F.cx1 && sy >= F.cy0 && sy < F.cy1;
     }
     if (p.x >= 0.0f && inRegion) {
-        float grx = scale * fx2_to_float(gh.x, (unsigned long long)gl.x, F.gradExp);
-        float gry = scale * fx2_to_float(gh.y, (unsigned long long)gl.y, F.gradExp);
         float2 m = F.m[i], v = F.v[i];
         float b1 = F.beta1, b2 = F.beta2;
         float mx = b1 * m.x + (1.0f - b1) * grx;
@@ -144,6 +165,24 @@ __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits
     int c = cell_coord(p.y, F.inv, F.gridH) * F.gridW + cell_coord(p.x, F.inv, F.gridW);
     F.key[i] = c;
     F.rank[i] = atomicAdd(&F.counts[c], 1);
+}
+
+// The largest number of targets in any 5x5 block of hash cells (the bound
+// behind a fit's fast-path split shift), from the target sort's key starts:
+// keys are cell << 2 sub, so a row of cells is one contiguous key range.
+__global__ void __launch_bounds__(256) k_block5_max(const int *__restrict__ tstart, int gw, int gh, int sub,
+                                                    int *out)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int sum = 0;
+    if (c < gw * gh) {
+        int y = c / gw, x = c - y * gw;
+        int xa = max(x - 2, 0), xb = min(x + 2, gw - 1);
+        for (int yy = max(y - 2, 0); yy <= min(y + 2, gh - 1); ++yy)
+            sum += tstart[(size_t)(yy * gw + xb + 1) << (2 * sub)] - tstart[(size_t)(yy * gw + xa) << (2 * sub)];
+    }
+    sum = __reduce_max_sync(kFull, sum);
+    if ((threadIdx.x & 31) == 0 && sum > 0) atomicMax(out, sum);
 }
 
 // Sparse target update (reference scatterTargetsKernel, voro_optimizer.cu:303-307)
@@ -250,6 +289,23 @@ cudaError_t vm_launch_knn(const VmFit *fit, const float2 *q, int nq, int K, int 
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+cudaError_t vm_launch_block5_max(const int *tstart, int gridW, int gridH, int sub, int *out, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int), s);
+    if (e) return e;
+    int cells = gridW * gridH;
+    k_block5_max<<<(cells + 255) / 256, 256, 0, s>>>(tstart, gridW, gridH, sub, out);
+    return cudaGetLastError();
+}
+
+float vm_fast_limit(int block5Max, int gradExp)
+{
+    double lim = std::ldexp(1.0, 62 - gradExp) / (double)(block5Max > 1 ? block5Max : 1);
+    float f = (float)lim;
+    if ((double)f > lim) f = std::nextafter(f, 0.0f); // rounded down, so the bound holds
+    return f;
 }
 
 cudaError_t vm_launch_scatter_targets(float2 *targets, const int *slots, const float2 *values, int n, cudaStream_t s)

@@ -29,8 +29,9 @@ struct VmState {
     int slowTotal;   // targets that needed the exact ring search (cumulative)
     int errors;      // error bits raised by kernels (see VM_KERR_*)
     float schedLr, schedBc1, schedBc2; // this step's learning rate and bias corrections
-    int clamped;     // gradient terms clamped to +-2^62 in fixed point (cumulative)
-    int pad[15];
+    int needExact;   // this pass's fast-path gradient bound failed: the whole gradient is redone exactly
+    int dUsed;       // this pass added to the exact split words (gradX sections DL, DH)
+    int pad[14];
 };
 
 enum : int {
@@ -54,10 +55,10 @@ struct VmFit {
     int gradExp, lossExp; // fixed-point exponents
     int nTargets;         // live targets in tpos/tslot (cell-sorted)
     int active;           // 1: stepped by this launch
-    int pad0;
+    float fastLimit;      // a gradient term at or above this flags the fit (see vm_fast_limit)
     // ---- device arrays ----
     VM_F2 *gen, *m, *v;   // slot order
-    long long *gradX;     // 4 per slot: exact split fixed-point sums {Lx, Ly, Hx, Hy}
+    long long *gradX;     // kGradWords per slot in three sections of 2 per slot: L, DL, DH
     int *key, *rank;      // per slot: grid cell (-1 empty) and rank within the cell
     int *counts;          // gridW*gridH (+1): per-cell counts, zero between builds
     int *start;           // gridW*gridH + 1: cell start in the sorted arrays
@@ -87,4 +88,4 @@ struct VmPointSet {
 };
 
 constexpr int kScanTile = 2048; // cells per scan tile (256 threads x 8)
-constexpr int kGradWords = 4;   // 64-bit words of exact gradient sums per slot {Lx, Ly, Hx, Hy}
+constexpr int kGradWords = 6;   // 64-bit words of exact gradient sums per slot (three sections of (x, y))

@@ -41,8 +41,7 @@ class vm_params(C.Structure):
 class vm_info_t(C.Structure):
     _fields_ = [("iteration", C.c_int), ("scheduleLength", C.c_int), ("numSlots", C.c_int),
                 ("targetCapacity", C.c_int), ("liveTargets", C.c_int), ("gridW", C.c_int), ("gridH", C.c_int),
-                ("lastBatchLoss", C.c_float), ("exactTargets", C.c_longlong),
-                ("clampedTerms", C.c_longlong)]
+                ("lastBatchLoss", C.c_float), ("exactTargets", C.c_longlong)]
 
 
 class vm_mesh_info(C.Structure):

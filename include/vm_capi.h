@@ -76,8 +76,6 @@ typedef struct {
     int gridW, gridH;     /* hash grid */
     float lastBatchLoss;  /* LastBatchLoss() */
     long long exactTargets; /* targets resolved by the exact ring search so far */
-    long long clampedTerms; /* gradient terms whose fixed-point image passed +-2^62 and was clamped
-                               there (only near-coincident sites produce them); 0 in practice */
 } vm_info_t;
 
 typedef struct {

@@ -1,5 +1,6 @@
 """Batched fits and serving: every fit's result equals the same fit run alone
-(bit for bit), in a batch of uneven sizes and in the served mix."""
+(bit for bit), in a batch of uneven sizes and in the served mix, and batch
+members and served requests equal the CPU oracle's fit."""
 import numpy as np
 import pytest
 
@@ -25,7 +26,18 @@ def alone(spec, steps):
     return g
 
 
-def test_batch_equals_alone(vm):
+def oracle_run(orc, spec, steps):
+    """The fit on the CPU oracle (the same arithmetic), with the schedule
+    params_for gives it; returns its generators after `steps` steps."""
+    ref = orc.Fit(spec.width, spec.height, spec.spacing, spec.lossK, spec.lrPerSpacing, spec.sampleFraction,
+                  spec.steps, nthreads=8)
+    ref.set_targets(spec.targets)
+    ref.set_generators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
+    ref.step(steps)
+    return ref.generators()[0]
+
+
+def test_batch_equals_alone(vm, orc):
     from voromesh_gb300.batch import Batch
 
     specs = small_batch()
@@ -35,6 +47,10 @@ def test_batch_equals_alone(vm):
     for fid, spec in zip(ids, specs):
         assert b.info(fid).iteration == 30
         assert np.array_equal(b.generators(fid), alone(spec, 30))
+    # batch members against the oracle: the smallest and the largest fit
+    sizes = [len(s.generators) for s in specs]
+    for k in (int(np.argmin(sizes)), int(np.argmax(sizes))):
+        assert np.array_equal(b.generators(ids[k]), oracle_run(orc, specs[k], 30))
     b.close()
 
 
@@ -71,7 +87,7 @@ def test_budget_admission(vm):
     b.close()
 
 
-def test_serve_equals_alone(vm):
+def test_serve_equals_alone(vm, orc):
     """Served results (continuous batching, staggered arrivals) equal each
     request run alone for the same number of steps."""
     from voromesh_gb300.batch import serve
@@ -83,6 +99,9 @@ def test_serve_equals_alone(vm):
     assert np.all(r.finished >= r.arrival)
     for spec, g in zip(specs, r.generators):
         assert np.array_equal(g, alone(spec, 40))
+    # a served request against the oracle
+    k = int(np.argmax([len(s.generators) for s in specs]))
+    assert np.array_equal(r.generators[k], oracle_run(orc, specs[k], 40))
     one = serve(specs, arrivals, hbm_budget=1 << 30, max_live=1, steps_per_round=10, max_steps=40, rel_tol=0.0)
     for g1, g2 in zip(one.generators, r.generators):
         assert np.array_equal(g1, g2)

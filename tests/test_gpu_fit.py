@@ -237,4 +237,41 @@ def test_gradient_sums_past_int64(vm, orc):
     om, ov = opt.Moments()
     assert np.array_equal(opt.Generators(), rg)
     assert np.array_equal(om, rm) and np.array_equal(ov, rv)
-    assert opt.info().clampedTerms == 0
+
+
+def _near_pair_fit():
+    """Two sites 5e-4 apart and 2^18 targets in a small cluster diagonal to
+    them, within the staged 5x5 block: every target resolves on the fast path
+    with large gradient terms (the sites nearly coincide), and two sites' sums
+    reach about 2^63.4 in fixed point."""
+    from voromesh_gb300 import synth
+
+    gen = np.array([[1.0, 1.0], [1.0005, 1.0], [0.3, 0.3], [1.7, 1.7]], np.float32)
+    tgt = (synth.uniform(24, 2, 1 << 18, -0.003, 0.003, shift=False) + np.float32([1.018, 1.018])).astype(np.float32)
+    return gen, tgt
+
+
+def test_fast_path_gradient_past_int64(vm, orc):
+    """A fit whose fast-path terms break the per-fit bound (most targets in a
+    5x5 block times the largest term): the fit is flagged, its gradient is
+    recomputed in the exact split words, and the result equals the oracle's
+    bit for bit and FP64 within 1e-6, with no target deferred."""
+    gen, tgt = _near_pair_fit()
+    opt, ref = _pair(vm, orc, gen, tgt, 0.05, 12, 0, 1.0, slots=(4, 1))
+    _, _, _, grad, cnt, _ = opt.Probe(0)
+    g, rcnt, _ = ref.gradient()
+    assert cnt == rcnt == len(tgt)
+    assert np.array_equal(grad, g)
+    d = orc.Fit64(2.0, 2.0, float(np.float32(0.05)), 12, 0.09, 1.0, 300)
+    d.set_targets(tgt)
+    d.set_generators(gen, 4, 1, 2.0)
+    g64, _, _ = d.gradient()
+    assert np.log2(np.abs(g64).max()) + orc.lib().vo_fixed_grad_exp(np.float32(0.05)) > 63.2
+    assert np.abs(grad - g64).max() <= 1e-6 * np.abs(g64).max()
+    opt.Step(3)
+    ref.step(3)
+    rg, rm, rv = ref.generators()
+    om, ov = opt.Moments()
+    assert np.array_equal(opt.Generators(), rg)
+    assert np.array_equal(om, rm) and np.array_equal(ov, rv)
+    assert opt.info().exactTargets == 0

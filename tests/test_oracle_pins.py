@@ -453,3 +453,24 @@ def test_local_edit_matches_live_reference(orc):
     assert np.array_equal(l1, rl1) and np.array_equal(l2, rl2)
     assert np.array_equal(g1, rg1) and np.array_equal(m1, rm1) and np.array_equal(v1, rv1)
     assert np.array_equal(g2, rg2) and np.array_equal(m2, rm2) and np.array_equal(v2, rv2)
+
+
+def test_fast_path_sums_past_int64_oracle(orc):
+    """Two nearly coincident sites and 2^18 targets beside them: per-site
+    fixed-point sums pass 2^63 and the oracle's gradient still equals FP64
+    within 1e-6."""
+    from voromesh_gb300 import synth
+
+    gen = np.array([[1.0, 1.0], [1.0005, 1.0], [0.3, 0.3], [1.7, 1.7]], np.float32)
+    tgt = (synth.uniform(24, 2, 1 << 18, -0.003, 0.003, shift=False) + np.float32([1.018, 1.018])).astype(np.float32)
+    f = orc.Fit(2.0, 2.0, 0.05, 12, 0.09, 1.0, 300, nthreads=8)
+    f.set_targets(tgt)
+    f.set_generators(gen, 4, 1, 2.0)
+    g, cnt, _ = f.gradient()
+    d = orc.Fit64(2.0, 2.0, float(np.float32(0.05)), 12, 0.09, 1.0, 300, nthreads=8)
+    d.set_targets(tgt)
+    d.set_generators(gen, 4, 1, 2.0)
+    g64, c64, _ = d.gradient()
+    assert cnt == c64 == len(tgt)
+    assert np.log2(np.abs(g64).max()) + orc.lib().vo_fixed_grad_exp(np.float32(0.05)) > 63.2
+    assert np.abs(g - g64).max() <= 1e-6 * np.abs(g64).max()
