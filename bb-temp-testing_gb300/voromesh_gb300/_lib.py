@@ -1,4 +1,5 @@
-"""Loads libvoromesh_gb300.so (built in-tree) and declares its C ABI.
+"""Loads libvoromesh_gb300.so (built in-tree) and declares its C ABI, and
+libvm_synth.so, the seeded input generators.
 
 There is no fallback: if the library is missing or cannot be loaded the
 import fails with an error that says how to build it.
@@ -10,6 +11,7 @@ import os
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libvoromesh_gb300.so"
+SYNTH_PATH = LIB_PATH.parent / "libvm_synth.so"
 
 VM_OK = 0
 ERRORS = {
@@ -131,7 +133,11 @@ SIGNATURES = {
     "vm_checkpoint": [P, P, P, P, P],
     "vm_restore": [P, P, P, P, P],
     "vm_update_from_canvas": [P, P],
-    # seeded generators (host only)
+}
+_RESTYPES = {"vm_error_string": C.c_char_p, "vm_params_default": None}
+
+# the seeded input generators (libvm_synth.so, host code)
+SYNTH_SIGNATURES = {
     "vm_synth_uniform": [C.c_uint64, C.c_uint64, C.c_int64, C.c_double, C.c_double, I, P],
     "vm_synth_circle": [C.c_uint64, C.c_uint64, C.c_int64, C.c_double, C.c_double, I, P],
     "vm_synth_lattice": [C.c_uint64, C.c_uint64, I, I, C.c_double, I, P],
@@ -144,10 +150,10 @@ SIGNATURES = {
     "vm_synth_log": [C.c_double],
     "vm_synth_exp": [C.c_double],
 }
-_RESTYPES = {"vm_error_string": C.c_char_p, "vm_params_default": None, "vm_synth_uniform": None,
-             "vm_synth_circle": None, "vm_synth_lattice": None, "vm_synth_ellipse_params": None,
-             "vm_synth_ellipse_union": C.c_int64, "vm_synth_star": None, "vm_synth_star_params": None,
-             "vm_synth_uniform01": C.c_double, "vm_synth_log": C.c_double, "vm_synth_exp": C.c_double}
+_SYNTH_RESTYPES = {"vm_synth_uniform": None, "vm_synth_circle": None, "vm_synth_lattice": None,
+                   "vm_synth_ellipse_params": None, "vm_synth_ellipse_union": C.c_int64, "vm_synth_star": None,
+                   "vm_synth_star_params": None, "vm_synth_subset": C.c_int, "vm_synth_uniform01": C.c_double,
+                   "vm_synth_log": C.c_double, "vm_synth_exp": C.c_double}
 
 _lib = None
 
@@ -167,6 +173,26 @@ def load() -> C.CDLL:
         fn.argtypes = args
         fn.restype = _RESTYPES.get(name, C.c_int)
     _lib = lib
+    return lib
+
+
+_synth = None
+
+
+def load_synth() -> C.CDLL:
+    """The seeded input generators (raises if they have not been built)."""
+    global _synth
+    if _synth is not None:
+        return _synth
+    if not SYNTH_PATH.exists():
+        raise ImportError(f"{SYNTH_PATH} not found: build it with "
+                          "`python -c 'import __graft_entry__ as g; g.build()'` at the repository root")
+    lib = C.CDLL(str(SYNTH_PATH))
+    for name, args in SYNTH_SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _SYNTH_RESTYPES.get(name, C.c_int)
+    _synth = lib
     return lib
 
 

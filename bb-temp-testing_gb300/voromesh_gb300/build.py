@@ -1,9 +1,12 @@
 """Builds libvoromesh_gb300.so in-tree (nvcc for sm_103a, parallel, no cmake).
 
 The library holds the CUDA kernels, the C ABI (include/vm_capi.h), the
-reference-compatible C++ classes (include/voromesh, include/poisson), the
-batched/serving runtime and the seeded input generators. Output:
-bb-temp-testing_gb300/voromesh_gb300/_lib/libvoromesh_gb300.so
+reference-compatible C++ classes (include/voromesh, include/poisson) and the
+batched/serving runtime. The seeded input generators (csrc/synth.c, host
+code) are a library of their own, libvm_synth.so, so that a program that
+only needs the inputs (the CPU baseline) does not load the GPU library.
+Outputs: bb-temp-testing_gb300/voromesh_gb300/_lib/libvoromesh_gb300.so and
+libvm_synth.so.
 """
 from __future__ import annotations
 
@@ -20,6 +23,7 @@ ROOT = PKG.parent.parent
 INCLUDE = ROOT / "include"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "libvoromesh_gb300.so"
+SYNTH_LIB = OUT_DIR / "libvm_synth.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: a*b+c stays two IEEE roundings in device code (the reference's
@@ -76,13 +80,17 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         workers = max(1, min(len(jobs), os.cpu_count() or 4))
         with cf.ThreadPoolExecutor(workers) as ex:
             list(ex.map(_run, jobs))
-    objs = [str(objdir / (s + ".o")) for s in CU_SOURCES + CXX_SOURCES + C_SOURCES if (CSRC / s).exists()]
+    objs = [str(objdir / (s + ".o")) for s in CU_SOURCES + CXX_SOURCES if (CSRC / s).exists()]
     if force or jobs or not LIB.exists():
         tmp = LIB.with_suffix(".so.tmp")
         _run([nvcc] + ARCH + ["-shared", "-o", str(tmp)] + objs + ["-lcudart"])
         os.replace(tmp, LIB)
+    if force or jobs or not SYNTH_LIB.exists():
+        tmp = SYNTH_LIB.with_suffix(".so.tmp")
+        _run(["gcc", "-shared", "-o", str(tmp)] + [str(objdir / (s + ".o")) for s in C_SOURCES] + ["-lm"])
+        os.replace(tmp, SYNTH_LIB)
     if verbose:
-        print(f"built {LIB}", file=sys.stderr)
+        print(f"built {LIB} and {SYNTH_LIB.name}", file=sys.stderr)
     return LIB
 
 

@@ -1,5 +1,5 @@
-"""Seeded synthetic workloads (generated by the library's portable C code, so
-the same seed gives the same bytes on every host).
+"""Seeded synthetic workloads (generated by portable C code, libvm_synth.so,
+so the same seed gives the same bytes on every host).
 
 Shapes are defined on [-1,1]^2 and shifted by +1 into the optimiser's
 [0,2]^2 domain. Nothing here is a public dataset: every workload is a
@@ -13,7 +13,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import load, ptr
+from ._lib import load_synth as load, ptr
 
 U64 = C.c_uint64
 

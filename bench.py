@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--reference-seconds", type=float, default=90.0,
+                    help="--impl reference: cap on the timed CPU work (full steps of the whole fit)")
+    ap.add_argument("--no-fits", action="store_true",
+                    help="default workload: leave out the uneven-batch and served-stream figures")
     ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit", "poisson", "canvas"],
                     help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads; "
                          "extract: the cell clipper; edit: the local-edit pipeline; poisson: the sampler; "
@@ -63,6 +67,8 @@ def parse():
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--requests", type=int, default=200)
     ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--serve-low-rate", type=float, default=20.0,
+                    help="served stream: also run the batched server at this arrival rate (below capacity)")
     ap.add_argument("--serve-budget-gb", type=int, default=64)
     ap.add_argument("--serve-max-targets", type=int, default=1 << 24,
                     help="live-target cap of the served stream's admission (0 = none)")
@@ -96,18 +102,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """dram read+write bytes per k_loss launch from the committed ncu summary."""
-    p = ROOT / "profiles" / "k_loss_scale_1m.md"
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+# DRAM traffic of one k_loss launch at this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum), from an ncu capture of the kernel as built now; it
+# is a recorded figure, not measured by this run.
+K_LOSS_TRAFFIC = {"bytes_per_launch": 72430592,
+                  "source": "ncu capture of k_loss<256,3> at the 1M-site workload, 2026-12-04 build"}
 
 
 class ClockSampler:
@@ -181,57 +180,44 @@ def cpu_fit_rate(spec, seconds: float, nthreads: int):
     return N_SITES * steps / dt, steps, dt
 
 
-def reference_sample(spec, parts: int = 4):
-    """A bounded sample of the 1M-site workload for the CPU arm: the sites and
-    targets inside one of parts x parts square windows of the domain (shifted
-    to the origin), the window whose target-to-site ratio is nearest the
-    whole fit's. Same spacing, density and k; 1/parts^2 of the work a step."""
-    w = spec.width / parts
-    gen, tgt = spec.generators, spec.targets
-    ratio = len(tgt) / max(1, int((gen[:, 0] >= 0).sum()))
-    best = None
-    for wy in range(parts):
-        for wx in range(parts):
-            lo = np.array([wx * w, wy * w], np.float32)
-            g_in = np.all((gen >= lo) & (gen < lo + w), axis=1)
-            t_in = np.all((tgt >= lo) & (tgt < lo + w), axis=1)
-            if g_in.sum() == 0:
-                continue
-            score = abs(t_in.sum() / g_in.sum() - ratio)
-            if best is None or score < best[0]:
-                best = (score, lo, g_in, t_in)
-    _, lo, g_in, t_in = best
-    g = np.ascontiguousarray(gen[g_in] - lo)
-    t = np.ascontiguousarray(tgt[t_in] - lo)
-    return w, g, t
-
-
 def run_reference(args, world, rank):
+    """The reference arm: the reference's algorithm on the CPU (the oracle's
+    restatement of its kernels, fixed-point sums, on every host thread), on
+    the same 1M-site fit. Each timed step is one full step of the whole fit;
+    the steps timed are capped so the run ends within a few minutes."""
     if rank != 0:
         return
     from oracle import oracle as orc
 
     nthreads = os.cpu_count() or 1
-    cells, _ = orc.poisson_fill(2.0, 2.0, RADIUS, 30, 1)
+    cells, _ = orc.poisson_fill(2.0, 2.0, RADIUS, 30, 1, nthreads=nthreads)
     spec = make_inputs(cells)
-    w, g, t = reference_sample(spec)
-    f = orc.Fit(w, w, spec.spacing, spec.lossK, spec.lrPerSpacing, 1.0, spec.steps, nthreads=nthreads)
-    f.set_targets(t)
-    f.set_generators(g, len(g), 1, 2.0 * w)
-    f.step(max(args.warmup, 0))
+    f = orc.Fit(spec.width, spec.height, spec.spacing, spec.lossK, spec.lrPerSpacing, 1.0, spec.steps,
+                nthreads=nthreads)
+    f.set_targets(spec.targets)
+    f.set_generators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
     t0 = time.perf_counter()
-    f.step(args.steps)
+    f.step(1)
+    one = time.perf_counter() - t0
+    budget = max(args.reference_seconds, one)
+    warm = max(0, min(args.warmup - 1, int(budget / 4 / one)))
+    f.step(warm)
+    steps = max(1, min(args.steps, int(budget / one)))
+    t0 = time.perf_counter()
+    f.step(steps)
     dt = time.perf_counter() - t0
-    v = len(g) * args.steps / dt
+    v = N_SITES * steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "site-steps/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "scale_1m: 1,048,576 generators (Poisson r=1e-3 subset), 8,388,608 targets on a "
-                               "64-ellipse union, k=16", "sites": N_SITES, "targets": N_TARGETS, "k": K},
+                               "64-ellipse union, k=16, lr 0.09 spacing, all targets every step",
+                   "sites": N_SITES, "targets": N_TARGETS, "k": K, "parallelism": f"replicas x{world}"},
         "cpu_baseline": {"value": v, "unit": "site-steps/s", "cores": nthreads, "kind": "port",
-                         "sample": f"each step: one full oracle step of a 1/16-area window of the 1M-site fit "
-                                   f"({len(g)} sites, {len(t)} targets, same spacing and k) on {nthreads} threads"},
+                         "sample": f"{steps} full steps of the whole 1M-site fit after {1 + warm} warm-up steps "
+                                   f"({dt:.1f} s on {nthreads} threads; steps capped at "
+                                   f"{args.reference_seconds:.0f} s of work)"},
         "e2e": {"value": v, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -241,15 +227,16 @@ def pct(a, q):
     return float(np.percentile(np.asarray(a), q)) if len(a) else None
 
 
-def run_batch(args):
-    """Uneven batch: 512 fits (generators log-uniform in [1,024, 262,144], 4x
-    targets on random star polygons, 200 steps each) in one batch, against the
-    one-fit-at-a-time loop on the same GPU. fits/s over uploads + steps."""
+def batch_figures(fits: int, fit_steps: int) -> dict:
+    """Uneven batch: `fits` fits (generators log-uniform in [1,024, 262,144],
+    4x targets on random star polygons, `fit_steps` steps each) in one batch,
+    against the one-fit-at-a-time loop on the same GPU. fits/s over uploads,
+    steps and the final loss read-back."""
     import voromesh_gb300 as vm
     from voromesh_gb300 import synth
     from voromesh_gb300.batch import Batch, fit_bytes, params_for
 
-    specs = synth.uneven_batch(n_fits=args.fits, steps=args.fit_steps)
+    specs = synth.uneven_batch(n_fits=fits, steps=fit_steps)
     total_sites = sum(s.slotsW * s.slotsH for s in specs)
     arena = int(sum(fit_bytes(s) for s in specs) * 1.05) + (64 << 20)
     # warm-up: one small batch (module load, tables)
@@ -262,12 +249,12 @@ def run_batch(args):
     for s in specs:
         b.add(s)
     t1 = time.perf_counter()
-    gpu_ms = b.step(args.fit_steps)
-    losses = b.evaluate()
+    gpu_ms = b.step(fit_steps)
+    b.evaluate()
     t2 = time.perf_counter()
     b.close()
     batched = {"fits_per_s": len(specs) / (t2 - t0), "wall_s": t2 - t0, "upload_s": t1 - t0,
-               "step_gpu_ms": gpu_ms, "site_steps_per_s": total_sites * args.fit_steps / (gpu_ms / 1e3)}
+               "step_gpu_ms": gpu_ms, "site_steps_per_s": total_sites * fit_steps / (gpu_ms / 1e3)}
     # plain loop: one VoroOptimizer at a time, each graph-stepped (the reference's usage pattern)
     t0 = time.perf_counter()
     gpu_plain = 0.0
@@ -275,14 +262,19 @@ def run_batch(args):
         o = vm.VoroOptimizer(s.width, s.height, s.spacing, params_for(s))
         o.SetTargets(s.targets)
         o.SetGenerators(s.generators, s.slotsW, s.slotsH, s.slotCellSize)
-        gpu_plain += o.Step(args.fit_steps)
+        gpu_plain += o.Step(fit_steps)
+        o.EvaluateLoss()
         o.close()
     t1 = time.perf_counter()
     plain = {"fits_per_s": len(specs) / (t1 - t0), "wall_s": t1 - t0, "step_gpu_ms": gpu_plain}
-    print(json.dumps({"metric": "fits/s, uneven batch", "workload": f"{len(specs)} fits, generators log-uniform "
-                      f"[1024, 262144] (sum {total_sites}), 4x targets on random stars, {args.fit_steps} steps each, k=16",
-                      "batched": batched, "plain_loop": plain, "speedup": batched["fits_per_s"] / plain["fits_per_s"],
-                      "unit": "fits/s", "data": "synthetic"}), flush=True)
+    return {"metric": "fits/s, uneven batch", "workload": f"{len(specs)} fits, generators log-uniform "
+            f"[1024, 262144] (sum {total_sites}), 4x targets on random stars, {fit_steps} steps each, k=16",
+            "batched": batched, "plain_loop": plain, "speedup": batched["fits_per_s"] / plain["fits_per_s"],
+            "unit": "fits/s", "data": "synthetic"}
+
+
+def run_batch(args):
+    print(json.dumps(batch_figures(args.fits, args.fit_steps)), flush=True)
 
 
 def run_extract(args):
@@ -520,19 +512,14 @@ def run_poisson(args):
                       "data": "synthetic"}), flush=True)
 
 
-def run_serve(args):
-    """Served stream: Poisson arrivals, generators log-uniform in [1k, 1M],
-    8x targets from the ellipse-union or star shapes (coin flip), retire at
-    500 steps or relative loss change < 1e-6; continuous batching vs the
-    one-fit-at-a-time loop; fits/s and p50/p99 arrival-to-result latency."""
+def serve_specs(n: int):
+    """The served stream's requests: generators log-uniform in [1k, 1M], 8x
+    targets cut from ellipse-union or star pools (coin flip)."""
     import concurrent.futures as cf
     import math
 
     from voromesh_gb300 import synth
-    from voromesh_gb300.batch import fit_bytes, serve
 
-    n = args.requests
-    arrivals = synth.arrival_times(1, n, args.rate)
     sizes = synth.log_uniform_ints(1, 17, n, 1024, 1048576)
     coin = synth.uniform01(1, 19, n)
     pool_n = int(8 * sizes.max())
@@ -549,25 +536,48 @@ def run_serve(args):
         tgt = np.ascontiguousarray(pool[off:off + 8 * s])
         gen = synth.uniform(1, 600000 + 3 * i, s)
         specs.append(synth.FitSpec(f"req_{i}", 2.0, 2.0, 2.0 / math.sqrt(s), gen, s, 1, 2.0, tgt, 16, 0.09, 500))
-    budget = args.serve_budget_gb << 30
+    return specs
+
+
+def serve_figures(n: int, rate: float, budget_gb: int, max_targets: int, low_rate: float = 0.0,
+                  capped: bool = True) -> dict:
+    """Served stream: Poisson arrivals at `rate`/s, retire at 500 steps or
+    relative loss change < 1e-6; continuous batching vs the one-fit-at-a-time
+    loop (maxLive = 1); fits/s and p50/p99 arrival-to-result latency. With
+    low_rate, the batched server also runs at that arrival rate (below its
+    capacity), so its p50/p99 are service times rather than queueing."""
+    from voromesh_gb300 import synth
+    from voromesh_gb300.batch import fit_bytes, serve
+
+    specs = serve_specs(n)
+    budget = budget_gb << 30
     need = max(fit_bytes(s) for s in specs)
     out = {}
-    # batched: admission by memory alone (throughput); batched_capped: a live-target
-    # cap as well, so early requests finish sooner (latency)
-    runs = (("batched", 4096, 0), ("batched_capped", 4096, args.serve_max_targets), ("plain_loop", 1, 0))
-    for name, live, cap in runs:
+    runs = [("batched", rate, 4096, 0)]
+    if capped:
+        runs.append(("batched_capped", rate, 4096, max_targets))
+    runs.append(("plain_loop", rate, 1, 0))
+    if low_rate > 0:
+        runs.append(("batched_below_capacity", low_rate, 4096, 0))
+    for name, r_rate, live, cap in runs:
+        arrivals = synth.arrival_times(1, n, r_rate)
         r = serve(specs, arrivals, budget, max_live=live, steps_per_round=10, max_steps=500, rel_tol=1e-6,
                   keep_generators=False, max_live_targets=cap)
         lat = r.latency
         span = float(r.finished.max() - r.arrival.min())
-        out[name] = {"fits_per_s": n / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99), "span_s": span,
-                     "mean_steps": float(r.steps.mean()), "rejected": int((r.status != 0).sum())}
-    print(json.dumps({"metric": "fits/s + p50/p99, served stream", "workload": f"{n} requests, Poisson arrivals "
-                      f"{args.rate}/s, generators log-uniform [1k, 1M], 8x targets (ellipse union or star), retire at "
-                      f"500 steps or rel loss change < 1e-6, HBM budget {args.serve_budget_gb} GiB "
-                      f"(batched_capped: live targets capped at {args.serve_max_targets})", **out,
-                      "speedup": out["batched"]["fits_per_s"] / out["plain_loop"]["fits_per_s"],
-                      "largest_fit_bytes": need, "unit": "fits/s", "data": "synthetic"}), flush=True)
+        out[name] = {"arrival_rate": r_rate, "fits_per_s": n / span, "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+                     "span_s": span, "mean_steps": float(r.steps.mean()), "rejected": int((r.status != 0).sum())}
+    return {"metric": "fits/s + p50/p99, served stream", "workload": f"{n} requests, Poisson arrivals "
+            f"{rate}/s, generators log-uniform [1k, 1M], 8x targets (ellipse union or star), retire at "
+            f"500 steps or rel loss change < 1e-6, HBM budget {budget_gb} GiB"
+            + (f" (batched_capped: live targets capped at {max_targets})" if capped else ""), **out,
+            "speedup": out["batched"]["fits_per_s"] / out["plain_loop"]["fits_per_s"],
+            "largest_fit_bytes": need, "unit": "fits/s", "data": "synthetic"}
+
+
+def run_serve(args):
+    print(json.dumps(serve_figures(args.requests, args.rate, args.serve_budget_gb, args.serve_max_targets,
+                                   args.serve_low_rate)), flush=True)
 
 
 def main():
@@ -627,7 +637,14 @@ def main():
     barrier()
     with ClockSampler(local) as clk:
         ms = opt.Step(args.steps)
-    barrier()
+        barrier()
+        # the same stepping load continues, untimed, until the sampler has at
+        # least 1 s of clock readings (a short timed region sees none)
+        t_load = time.perf_counter()
+        while clk.proc is not None and (time.perf_counter() - t_load < 1.2 or len(clk.samples) < 8):
+            opt.Step(max(1, min(args.steps, 200)))
+            if time.perf_counter() - t_load > 10:
+                break
     ms, value = job_rate(ms, N_SITES * args.steps, world, dist, "cuda")
 
     # ---- roofline of the loss kernel (stage events around each kernel)
@@ -637,7 +654,6 @@ def main():
     peak, peak_kind = measured_peaks()
     stepBytes = 88 * N_SITES + 8 * N_TARGETS + 8 * opt.info().gridW * opt.info().gridH
     achieved = lossBytes / (loss_ms / 1e3) / 1e9
-    traffic = ncu_traffic()
     info = opt.info()
 
     # ---- e2e: the public API from pinned host buffers
@@ -657,6 +673,17 @@ def main():
     e2e = N_SITES * args.steps * world / e2e_s
     h2d = (spec.targets.nbytes + spec.generators.nbytes) / args.steps
     d2h = 128 + spec.generators.nbytes / args.steps
+
+    # ---- fits/s: the uneven batch and the served stream (rank 0, N=1)
+    fits = None
+    loss_variant = opt.LossVariant()[0]
+    if rank == 0 and world == 1 and not args.no_fits:
+        opt.close()
+        batch = batch_figures(args.fits, args.fit_steps)
+        srv = serve_figures(args.requests, args.rate, args.serve_budget_gb, args.serve_max_targets,
+                            args.serve_low_rate, capped=False)
+        fits = {"batch": {k: batch[k] for k in ("workload", "batched", "plain_loop", "speedup")},
+                "serve": {k: v for k, v in srv.items() if k not in ("metric", "unit", "data")}}
 
     # ---- CPU baseline (rank 0, N=1): the oracle on a bounded sample
     cpu = None
@@ -680,15 +707,17 @@ def main():
                        "poisson_fill": {"samples": n_samples, "ms": fill_ms, "samples_per_s": n_samples / (fill_ms / 1e3)},
                        "stage_ms": {"loss": float(stages[0]), "adam_bin": float(stages[1]),
                                     "scan": float(stages[2]), "scatter": float(stages[3])},
-                       "exact_path_targets": int(info.exactTargets), "loss_variant": opt.LossVariant()[0]},
+                       "exact_path_targets": int(info.exactTargets), "loss_variant": loss_variant},
             "e2e": {"value": e2e, "unit": "site-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": "k_loss", "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": K_LOSS_TRAFFIC["bytes_per_launch"], "traffic_source": K_LOSS_TRAFFIC["source"],
                          "algorithmic_bytes_per_launch": lossBytes, "mean_launch_ms": loss_ms},
             # the whole step against HBM: B_step = 88 B per site + 8 B per target + 8 B per cell
             "step_roofline": {"bytes_per_step": stepBytes, "achieved": stepBytes / (ms / args.steps) / 1e6,
                               "unit": "GB/s", "frac": stepBytes / (ms / args.steps) / 1e6 / peak},
             "cpu_baseline": cpu,
+            "fits": fits,
             "clocks": clk.summary(),
             "gpu_launches": KERNELS_PER_STEP * args.steps,
         }

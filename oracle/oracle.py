@@ -68,6 +68,7 @@ def lib() -> C.CDLL:
         _lib.vo_fit64_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.vo_fit64_detail.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.vo_poisson_resample.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
+        _lib.vo_poisson_resample_mt.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.vo_poisson_verify.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
         _lib.vo_poisson_init.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_int, C.c_uint]
         _lib.vo_extract_cells.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_int,
@@ -348,15 +349,15 @@ class Fit64:
         return i0, j
 
 
-def poisson_fill(width, height, radius, trials=30, seed=1, regions=()):
+def poisson_fill(width, height, radius, trials=30, seed=1, regions=(), nthreads=1):
     """Sampler construction (full fill) followed by Resample() of each region."""
     p = VoPoisson()
     L = lib()
     L.vo_poisson_init(C.byref(p), width, height, radius, trials, seed)
     grid = np.full((p.gridW * p.gridH, 2), -1.0, np.float32)
-    L.vo_poisson_resample(C.byref(p), P(grid), 0, 0, p.gridW, p.gridH)
+    L.vo_poisson_resample_mt(C.byref(p), P(grid), 0, 0, p.gridW, p.gridH, nthreads)
     for (x0, y0, x1, y1) in regions:
-        L.vo_poisson_resample(C.byref(p), P(grid), x0, y0, x1, y1)
+        L.vo_poisson_resample_mt(C.byref(p), P(grid), x0, y0, x1, y1, nthreads)
     return grid, p
 
 

@@ -37,7 +37,7 @@ static void *vo_job_run(void *arg)
 
 static void vo_parallel(int nthreads, int64_t n, vo_range_fn fn, void *ctx)
 {
-    if (nthreads <= 1 || n < 1024) {
+    if (nthreads <= 1 || n < 2 * (int64_t)nthreads) {
         fn(ctx, 0, n, 0);
         return;
     }
@@ -1436,7 +1436,53 @@ void vo_poisson_init(vo_poisson *p, float width, float height, float radius, int
     p->roundBase = 0;
 }
 
-void vo_poisson_resample(vo_poisson *p, vo_f2 *grid, int cx0, int cy0, int cx1, int cy1)
+/* One phase of one round over rows [lo, hi) of the phase's rows: a dart per
+ * empty phase cell, rejected if any sample of the 5x5 neighbourhood is nearer
+ * than the radius (dartPhaseKernel, poisson_disk.cu:74-107). Cells of a phase
+ * are 3 apart and read only cells of other phases, so rows of a phase can run
+ * in parallel with the same result as in order. */
+typedef struct {
+    const vo_poisson *p;
+    vo_f2 *grid;
+    int x0, x1, y0, px, py;
+    unsigned rnd;
+} vo_phase_job;
+
+static void poisson_phase_rows(void *ctx, int64_t lo, int64_t hi, int tid)
+{
+    (void)tid;
+    const vo_phase_job *J = (const vo_phase_job *)ctx;
+    const vo_poisson *p = J->p;
+    vo_f2 *grid = J->grid;
+    float r2 = p->radius * p->radius;
+    for (int64_t row = lo; row < hi; ++row) {
+        int cy = J->y0 + J->py + 3 * (int)row;
+        for (int cx = J->x0 + J->px; cx < J->x1; cx += 3) {
+            int cellId = cy * p->gridW + cx;
+            if (grid[cellId].x >= 0.0f) continue;
+            float x = ((float)cx + vo_poisson_rand01((unsigned)cellId, J->rnd, p->seed, 0)) * p->cellSize;
+            float y = ((float)cy + vo_poisson_rand01((unsigned)cellId, J->rnd, p->seed, 1)) * p->cellSize;
+            if (x >= p->width || y >= p->height) continue;
+            int nx0 = cx - 2 > 0 ? cx - 2 : 0, nx1 = cx + 2 < p->gridW - 1 ? cx + 2 : p->gridW - 1;
+            int ny0 = cy - 2 > 0 ? cy - 2 : 0, ny1 = cy + 2 < p->gridH - 1 ? cy + 2 : p->gridH - 1;
+            int reject = 0;
+            for (int ny = ny0; ny <= ny1 && !reject; ++ny)
+                for (int nx = nx0; nx <= nx1; ++nx) {
+                    vo_f2 q = grid[(size_t)ny * p->gridW + nx];
+                    if (q.x < 0.0f) continue;
+                    float dx = q.x - x, dy = q.y - y;
+                    if (dx * dx + dy * dy < r2) { reject = 1; break; }
+                }
+            if (reject) continue;
+            grid[cellId].x = x;
+            grid[cellId].y = y;
+        }
+    }
+}
+
+/* Sampler::Resample (poisson_disk.cu:141-177): clear the region, then
+ * trials rounds of 9 phases (3x3 colour classes). */
+void vo_poisson_resample_mt(vo_poisson *p, vo_f2 *grid, int cx0, int cy0, int cx1, int cy1, int nthreads)
 {
     int x0 = cx0 > 0 ? cx0 : 0, y0 = cy0 > 0 ? cy0 : 0;
     int x1 = cx1 < p->gridW ? cx1 : p->gridW, y1 = cy1 < p->gridH ? cy1 : p->gridH;
@@ -1446,34 +1492,21 @@ void vo_poisson_resample(vo_poisson *p, vo_f2 *grid, int cx0, int cy0, int cx1, 
             grid[(size_t)y * p->gridW + x].x = -1.0f;
             grid[(size_t)y * p->gridW + x].y = -1.0f;
         }
-    float r2 = p->radius * p->radius;
-    for (int round = 0; round < p->trials; ++round) {
-        unsigned rnd = p->roundBase + (unsigned)round;
+    for (int round = 0; round < p->trials; ++round)
         for (int py = 0; py < 3; ++py)
-            for (int px = 0; px < 3; ++px)
-                for (int cy = y0 + py; cy < y1; cy += 3)
-                    for (int cx = x0 + px; cx < x1; cx += 3) {
-                        int cellId = cy * p->gridW + cx;
-                        if (grid[cellId].x >= 0.0f) continue;
-                        float x = ((float)cx + vo_poisson_rand01((unsigned)cellId, rnd, p->seed, 0)) * p->cellSize;
-                        float y = ((float)cy + vo_poisson_rand01((unsigned)cellId, rnd, p->seed, 1)) * p->cellSize;
-                        if (x >= p->width || y >= p->height) continue;
-                        int nx0 = cx - 2 > 0 ? cx - 2 : 0, nx1 = cx + 2 < p->gridW - 1 ? cx + 2 : p->gridW - 1;
-                        int ny0 = cy - 2 > 0 ? cy - 2 : 0, ny1 = cy + 2 < p->gridH - 1 ? cy + 2 : p->gridH - 1;
-                        int reject = 0;
-                        for (int ny = ny0; ny <= ny1 && !reject; ++ny)
-                            for (int nx = nx0; nx <= nx1; ++nx) {
-                                vo_f2 q = grid[(size_t)ny * p->gridW + nx];
-                                if (q.x < 0.0f) continue;
-                                float dx = q.x - x, dy = q.y - y;
-                                if (dx * dx + dy * dy < r2) { reject = 1; break; }
-                            }
-                        if (reject) continue;
-                        grid[cellId].x = x;
-                        grid[cellId].y = y;
-                    }
-    }
+            for (int px = 0; px < 3; ++px) {
+                vo_phase_job J = {p, grid, x0, x1, y0, px, py, p->roundBase + (unsigned)round};
+                int rows = y0 + py < y1 ? (y1 - 1 - (y0 + py)) / 3 + 1 : 0;
+                int nt = nthreads;
+                if ((int64_t)rows * ((x1 - x0 + 2) / 3) < 65536) nt = 1; /* small phases: no threads */
+                vo_parallel(nt, rows, poisson_phase_rows, &J);
+            }
     p->roundBase += (unsigned)p->trials;
+}
+
+void vo_poisson_resample(vo_poisson *p, vo_f2 *grid, int cx0, int cy0, int cx1, int cy1)
+{
+    vo_poisson_resample_mt(p, grid, cx0, cy0, cx1, cy1, 1);
 }
 
 /* Sampler::Verify: poisson_disk.cu:179-199 */

@@ -178,6 +178,9 @@ typedef struct {
 } vo_poisson;
 void vo_poisson_init(vo_poisson *p, float width, float height, float radius, int trials, unsigned seed);
 void vo_poisson_resample(vo_poisson *p, vo_f2 *grid, int cx0, int cy0, int cx1, int cy1);
+/* The same with the rows of each phase split over nthreads threads (the same
+ * result: cells of a phase are independent). */
+void vo_poisson_resample_mt(vo_poisson *p, vo_f2 *grid, int cx0, int cy0, int cx1, int cy1, int nthreads);
 int vo_poisson_verify(const vo_poisson *p, const vo_f2 *grid, int cx0, int cy0, int cx1, int cy1);
 
 /* ---- RNG (voro_optimizer.cu:69-78, poisson_disk.cu:47-58) ------------------ */

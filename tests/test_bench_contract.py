@@ -1,5 +1,5 @@
-"""bench.py's reference arm on the CPU: one bounded oracle step of the 1M-site
-workload's window sample, printed as the one JSON line of the bench contract
+"""bench.py's reference arm on the CPU: one full oracle step of the 1M-site
+workload, printed as the one JSON line of the bench contract
 (same metric and unit as the GPU arm, a cpu_baseline describing the run and
 an e2e object with no host-device traffic)."""
 import json
@@ -25,3 +25,15 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["sites"] == bench.N_SITES and d["config"]["targets"] == bench.N_TARGETS
+
+
+def test_reference_arm_loads_no_gpu_library():
+    """The reference arm's inputs come from libvm_synth.so and its steps from
+    the oracle: the GPU library is never loaded."""
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0']; "
+            "import bench; bench.main(); maps = open('/proc/self/maps').read(); "
+            "print('GPU_LIB_LOADED' if 'libvoromesh_gb300' in maps else 'GPU_LIB_ABSENT'); "
+            "print('SYNTH_LOADED' if 'libvm_synth' in maps else 'SYNTH_ABSENT')")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "GPU_LIB_ABSENT" in r.stdout and "SYNTH_LOADED" in r.stdout
