@@ -59,8 +59,8 @@ def parse():
                     help="--impl reference: cap on the timed CPU work (full steps of the whole fit)")
     ap.add_argument("--no-fits", action="store_true",
                     help="default workload: leave out the uneven-batch and served-stream figures")
-    ap.add_argument("--workload", default="scale", choices=["scale", "batch", "serve", "extract", "edit", "poisson", "canvas"],
-                    help="scale: the 1M-site fit (the headline line); batch / serve: fits/s workloads; "
+    ap.add_argument("--workload", default="scale", choices=["scale", "plain", "batch", "serve", "extract", "edit", "poisson", "canvas"],
+                    help="scale: the 1M-site fit (the headline line); plain: the 2,048-site fit; batch / serve: fits/s workloads; "
                          "extract: the cell clipper; edit: the local-edit pipeline; poisson: the sampler; "
                          "canvas: RasterizeShape and StampDisc")
     ap.add_argument("--fits", type=int, default=512)
@@ -275,6 +275,50 @@ def batch_figures(fits: int, fit_steps: int) -> dict:
 
 def run_batch(args):
     print(json.dumps(batch_figures(args.fits, args.fit_steps)), flush=True)
+
+
+def run_plain(args):
+    """The plain single fit: 2,048 generators uniform in [-1,1]^2, 16,384
+    targets on the circle r = 0.6 with N(0, 1e-3) radial noise, k = 12, cell
+    0.05, lr 1e-3, 300 steps. fits/s through the C ABI (upload, 300 steps,
+    fitted generators back), the resident step time and its stages, and the
+    CPU oracle on the same fit."""
+    import voromesh_gb300 as vm
+    from oracle import oracle as orc
+    from voromesh_gb300 import synth
+
+    spec = synth.plain_fit()
+    params = vm.OptimizerParams(iterations=spec.steps, sampleFraction=1.0, lrPerSpacing=spec.lrPerSpacing,
+                                lossK=spec.lossK)
+    opt = vm.VoroOptimizer(spec.width, spec.height, spec.spacing, params)
+    opt.SetTargets(spec.targets)
+    opt.SetGenerators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
+    opt.Step(20)  # warm-up (and the autotuner's pick)
+    reps = max(1, args.steps // spec.steps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        opt.SetTargets(spec.targets)
+        opt.SetGenerators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
+        gpu_ms = opt.Step(spec.steps)
+        opt.Generators()
+    wall = (time.perf_counter() - t0) / reps
+    stages = opt.StepTimed(spec.steps)
+    opt.close()
+    nthreads = os.cpu_count() or 1
+    f = orc.Fit(spec.width, spec.height, spec.spacing, spec.lossK, spec.lrPerSpacing, 1.0, spec.steps,
+                nthreads=nthreads)
+    f.set_targets(spec.targets)
+    f.set_generators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
+    t0 = time.perf_counter()
+    f.step(spec.steps)
+    cpu = time.perf_counter() - t0
+    print(json.dumps({"metric": "fits/s, plain single fit", "workload": "2,048 generators, 16,384 circle targets, "
+                      "k=12, cell 0.05, lr 1e-3, 300 steps", "fits_per_s": 1.0 / wall, "wall_ms_per_fit": wall * 1e3,
+                      "gpu_ms_per_step": gpu_ms / spec.steps,
+                      "stage_ms": {"loss": float(stages[0]), "adam_bin": float(stages[1]), "scan": float(stages[2]),
+                                   "scatter": float(stages[3])},
+                      "cpu_baseline": {"fits_per_s": 1.0 / cpu, "cores": nthreads, "kind": "port"},
+                      "unit": "fits/s", "data": "synthetic"}), flush=True)
 
 
 def run_extract(args):
@@ -585,6 +629,9 @@ def main():
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "plain":
+        run_plain(args)
         return
     if args.workload == "batch":
         run_batch(args)

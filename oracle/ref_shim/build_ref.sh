@@ -16,7 +16,7 @@
 # Usage: REF=/path/to/reference bash oracle/ref_shim/build_ref.sh
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${REF:-/root/reference}"
+REF="${REF:?set REF to the root of the reference project sources}"
 OUT="$HERE/../_ref"
 VORO="$REF/src/voromesh/voro_optimizer.cu"
 POIS="$REF/src/poisson/poisson_disk.cu"
