@@ -487,7 +487,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     releaseTmp();
     f.liveTargets = live;
     D.nTargets = live;
-    D.fastLimit = vm_fast_limit(b5, D.gradExp);
+    D.fastShift = vm_fast_shift(b5);
     if ((rc = single_set_build(b, f.sites, 1, 1))) { // the grid of the initial generators
         release_fit(b, f);
         return rc;

@@ -52,13 +52,23 @@ __device__ __forceinline__ float rand01(unsigned index, unsigned iter, unsigned 
 // order in which targets, warps or blocks contribute.
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
 
+// The loss kernel's per-block flag: it met a gradient term beyond its fit's
+// fastShift (see fx_from_float_any and vm_loss.cu).
+__shared__ int sFastOver;
+
 // round-half-even(v * 2^e) as int64, saturating at +-2^62, NaN -> 0; integer
 // operations only (64-bit float->int conversions run on the narrow FP64 pipe).
-static __device__ __noinline__ long long fx_from_float_any(float v, int e)
+// A term of 2^(fastShift + 24) or more (an infinite one included) raises
+// the block's sFastOver; callers that do not check it pass fastShift = 64.
+static __device__ __noinline__ long long fx_from_float_any(float v, int e, int fastShift)
 {
     unsigned u = __float_as_uint(v);
     int ex = (int)((u >> 23) & 0xFFu);
-    if (ex == 0xFF) return (u & 0x7FFFFFu) ? 0 : ((u >> 31) ? -4611686018427387904LL : 4611686018427387904LL);
+    if (ex == 0xFF) {
+        if (u & 0x7FFFFFu) return 0;
+        if (fastShift < 64) sFastOver = 1;
+        return (u >> 31) ? -4611686018427387904LL : 4611686018427387904LL;
+    }
     unsigned m = u & 0x7FFFFFu;
     int k; // |v| 2^e = m 2^k
     if (ex == 0) { // subnormal v
@@ -68,6 +78,7 @@ static __device__ __noinline__ long long fx_from_float_any(float v, int e)
         m |= 0x800000u;
         k = ex - 150 + e;
     }
+    if (ex != 0 && k > fastShift) sFastOver = 1;
     long long mag;
     if (k >= 0) {
         mag = k > 38 ? 4611686018427387904LL : ((long long)m << k);
@@ -95,7 +106,7 @@ __device__ __forceinline__ long long fx_from_float(float v, int e)
         long long mag = (long long)((u & 0x7FFFFFu) | 0x800000u) << k;
         return (u >> 31) ? -mag : mag;
     }
-    return fx_from_float_any(v, e);
+    return fx_from_float_any(v, e, 64);
 }
 
 __device__ __forceinline__ float fx_to_float(long long v, int e) { return __ll2float_rn(v) * pow2f(-e); }
@@ -109,18 +120,20 @@ __device__ __forceinline__ float fx_to_float(long long v, int e) { return __ll2f
 //           The fast path gives a target only sites of the 5x5 cell block
 //           around its own cell, so a site receives at most T5 terms (T5: the
 //           most live targets in any 5x5 block) and |S| <= T5 * max|term|.
-//           Every term is compared with the fit's fastLimit, 2^62 / (T5 2^e)
-//           rounded down (vm_fast_limit): below it no site sum can leave the
-//           int64 range, so L holds S itself. A warp that meets a term at or
-//           above it flags the fit, and the fit's whole gradient is
-//           recomputed into DL/DH instead (k_loss_exact), with L ignored.
+//           The loss kernel converts terms below 2^(fastShift + 24) inline,
+//           with fastShift = 38 - ceil(log2 T5) (vm_fast_shift), so those are
+//           below 2^62 / T5 and no site sum can leave the int64 range: L
+//           holds S itself. A larger term takes the out-of-line conversion,
+//           which flags the block; the fit's whole gradient is then
+//           recomputed into DL/DH (k_loss_exact), with L ignored.
 //   DL, DH  the deferred (ring-search) targets and flagged fits, in the
 //           unconditional split x = hi * 2^32 + lo, lo in [0, 2^32): a site
 //           receives fewer than 2^31 terms, so neither word wraps.
 //
 // So every site sum is exact for any input, and the fast path costs one
-// 64-bit reduction per component and one comparison per target. At the
-// 1M-site workload T5 * max|term| is about 2^54.6, far below 2^62.
+// 64-bit reduction per component; the bound costs no instruction on the
+// common path. At the 1M-site workload fastShift = 24 (terms up to 2^48)
+// and the largest term is 2^40.7.
 
 __host__ __device__ __forceinline__ float vm_pow2f(int e)
 {

@@ -33,10 +33,10 @@ cudaError_t vm_launch_knn(const VmFit *fit, const float2 *q, int nq, int K, int 
 int vm_loss_occupancy_blocks(int variant);
 cudaError_t vm_launch_scatter_targets(float2 *targets, const int *slots, const float2 *values, int n, cudaStream_t s);
 // The largest target count of any 5x5 block of cells (*out, device int) from
-// a target sort's key starts (sub-cell depth sub), and the fit's fastLimit
-// from it: the largest float f with f * 2^gradExp * max(block5Max, 1) <= 2^62.
+// a target sort's key starts (sub-cell depth sub), and the fit's fastShift
+// from it: 38 - ceil(log2 block5Max), so 2^(fastShift + 24) * block5Max <= 2^62.
 cudaError_t vm_launch_block5_max(const int *tstart, int gridW, int gridH, int sub, int *out, cudaStream_t s);
-float vm_fast_limit(int block5Max, int gradExp);
+int vm_fast_shift(int block5Max);
 
 // Voronoi cells for extraction (vm_extract.cu); vm_launch_compact_cells packs
 // the fixed-size cell slots into CSR order (start: n + 1 offsets).

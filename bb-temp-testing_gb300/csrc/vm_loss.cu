@@ -519,7 +519,10 @@ __device__ __forceinline__ void load_fit(const VmFit *__restrict__ fits, int f, 
     const int *src = reinterpret_cast<const int *>(&fits[f]);
     int *dst = reinterpret_cast<int *>(&sF);
     for (int i = threadIdx.x; i < (int)(sizeof(VmFit) / 4); i += blockDim.x) dst[i] = __ldg(&src[i]);
-    if (threadIdx.x == 0) sIter = (unsigned)(fits[f].state->iter + 1);
+    if (threadIdx.x == 0) {
+        sIter = (unsigned)(fits[f].state->iter + 1);
+        sFastOver = 0;
+    }
     __syncthreads();
 }
 
@@ -554,9 +557,27 @@ __device__ __forceinline__ void run_add(RunSum &r, int site, long long x, long l
     r.y += y;
 }
 
-// A warp whose lanes met a gradient term at or above the fit's fastLimit
-// (every term below it keeps every site sum below 2^62) flags the fit, once,
-// for the exact recomputation.
+// The loss kernel's fixed-point conversion of a gradient term. Its inline
+// path takes terms that are an integer significand shifted by at most the
+// fit's fastShift, so below 2^(fastShift + 24) <= 2^62 / T5: with every term
+// there, no site sum can leave the int64 range. Every other term goes
+// through the out-of-line conversion, which also raises the block's
+// sFastOver when the term is that large or larger, so the check costs
+// nothing on the common path.
+__device__ __forceinline__ long long fx_term(float v, int e, int fastShift)
+{
+    unsigned u = __float_as_uint(v);
+    int ex = (int)((u >> 23) & 0xFFu);
+    int k = ex - 150 + e;
+    if ((unsigned)(ex - 1) < 254u && (unsigned)k <= (unsigned)fastShift) {
+        long long mag = (long long)((u & 0x7FFFFFu) | 0x800000u) << k;
+        return (u >> 31) ? -mag : mag;
+    }
+    return fx_from_float_any(v, e, fastShift);
+}
+
+// A block that met a gradient term beyond the fit's fastShift flags the fit,
+// once, for the exact recomputation.
 __device__ __forceinline__ void flag_fit(const VmFit &F, int f, SlowQueue *queue)
 {
     if (atomicExch(&F.state->needExact, 1) == 0) {
@@ -609,7 +630,6 @@ __global__ void __launch_bounds__(THREADS, MINB)
         int aCnt = 0, aSlow = 0;
         unsigned long long *G = reinterpret_cast<unsigned long long *>(F.gradX);
         RunSum run0, runJ;
-        bool overLimit = false; // this lane met a gradient term at or above F.fastLimit
         for (int base = w0; base < w1; base += 32) {
             int local = base + lane;
             bool valid = local < w1;
@@ -697,18 +717,14 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 add128(aLo, aHi, lo, hi);
                 aCnt += 1;
                 if (mode == 0) {
-                    int e = F.gradExp;
-                    run_add(run0, o.i0, fx_from_float(o.g0x, e), fx_from_float(o.g0y, e), G);
-                    run_add(runJ, o.j, fx_from_float(o.gjx, e), fx_from_float(o.gjy, e), G);
-                    // (an infinite term is over; a NaN term converts to 0 and compares false)
-                    overLimit |= fmaxf(fmaxf(fabsf(o.g0x), fabsf(o.g0y)), fmaxf(fabsf(o.gjx), fabsf(o.gjy))) >=
-                                 F.fastLimit;
+                    int e = F.gradExp, fs = F.fastShift;
+                    run_add(run0, o.i0, fx_term(o.g0x, e, fs), fx_term(o.g0y, e, fs), G);
+                    run_add(runJ, o.j, fx_term(o.gjx, e, fs), fx_term(o.gjy, e, fs), G);
                 }
             }
         }
         run_flush(run0, G);
         run_flush(runJ, G);
-        if (__any_sync(kFull, overLimit) && lane == 0) flag_fit(F, f, queue);
         // the loss, count and fallbacks of this fit: warp, block, then one atomic each
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
@@ -733,6 +749,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 cnt += sCnt[w];
                 slow += sSlow[w];
             }
+            if (mode == 0 && sFastOver) flag_fit(F, f, queue);
             VmState *st = F.state;
             atomic_add128(&st->accLo, &st->accHi, lo, hi);
             if (cnt) atomicAdd(&st->accCount, cnt);

@@ -161,7 +161,7 @@ int upload_tables(vm_optimizer *h)
     F.lossExp = 64 - 2 * floor_log2f(h->spacing);
     F.nTargets = h->liveTargets;
     F.active = 1;
-    F.fastLimit = vm_fast_limit(h->block5Max, F.gradExp);
+    F.fastShift = vm_fast_shift(h->block5Max);
     F.gen = h->gen.p; F.m = h->m.p; F.v = h->v.p; F.gradX = h->gradX.p;
     F.key = h->key.p; F.rank = h->rank.p; F.counts = h->counts.p; F.start = h->start.p; F.tileSums = h->tileSums.p;
     F.sortedIdx = h->sortedIdx.p; F.sortedPos = h->sortedPos.p;

@@ -300,12 +300,11 @@ cudaError_t vm_launch_block5_max(const int *tstart, int gridW, int gridH, int su
     return cudaGetLastError();
 }
 
-float vm_fast_limit(int block5Max, int gradExp)
+int vm_fast_shift(int block5Max)
 {
-    double lim = std::ldexp(1.0, 62 - gradExp) / (double)(block5Max > 1 ? block5Max : 1);
-    float f = (float)lim;
-    if ((double)f > lim) f = std::nextafter(f, 0.0f); // rounded down, so the bound holds
-    return f;
+    int bits = 0; // ceil(log2(max(block5Max, 1)))
+    while (bits < 31 && (1LL << bits) < (long long)block5Max) ++bits;
+    return 38 - bits;
 }
 
 cudaError_t vm_launch_scatter_targets(float2 *targets, const int *slots, const float2 *values, int n, cudaStream_t s)

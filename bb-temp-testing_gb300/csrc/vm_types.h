@@ -55,7 +55,7 @@ struct VmFit {
     int gradExp, lossExp; // fixed-point exponents
     int nTargets;         // live targets in tpos/tslot (cell-sorted)
     int active;           // 1: stepped by this launch
-    float fastLimit;      // a gradient term at or above this flags the fit (see vm_fast_limit)
+    int fastShift;        // a gradient term of 2^(fastShift + 24) or more flags the fit (see vm_fast_shift)
     // ---- device arrays ----
     VM_F2 *gen, *m, *v;   // slot order
     long long *gradX;     // kGradWords per slot in three sections of 2 per slot: L, DL, DH
