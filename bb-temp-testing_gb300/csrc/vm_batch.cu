@@ -306,7 +306,7 @@ size_t vmb_fit_bytes(int slotsW, int slotsH, int nTargets, float width, float he
     size_t cells = gw * gh, tiles = (cells + kScanTile - 1) / kScanTile;
     n = std::max<size_t>(n, 1);
     return aligned(8 * n) * 3 + aligned(8 * kGradWords * n) + aligned(4 * n) * 3 + aligned(8 * n) + aligned(4 * (cells + 1)) * 2 +
-           aligned(4 * (tiles + 1)) + aligned(8 * cap) * 2 + aligned(4 * cap) * 3 + 8 * cap /* queue share */;
+           aligned(8 * (tiles + 1)) + aligned(8 * cap) * 2 + aligned(4 * cap) * 3 + 8 * cap /* queue share */;
 }
 
 int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
@@ -356,7 +356,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     // ---- memory: all-or-nothing from the arena
     size_t nn = std::max(n, 1);
     size_t sizes[] = {8 * nn, 8 * nn, 8 * nn, 8 * kGradWords * nn, 4 * nn, 4 * nn, 4 * nn, 8 * nn, 4 * ((size_t)f.cells + 1),
-                      4 * ((size_t)f.cells + 1), 4 * ((size_t)f.tiles + 1), 8 * (size_t)f.cap, 4 * (size_t)f.cap,
+                      4 * ((size_t)f.cells + 1), 8 * ((size_t)f.tiles + 1), 8 * (size_t)f.cap, 4 * (size_t)f.cap,
                       4 * (size_t)f.cap, 8 * (size_t)f.cap, 4 * (size_t)f.cap};
     char *ptrs[16];
     for (int k = 0; k < 16; ++k) {
@@ -389,7 +389,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     D.sortedPos = reinterpret_cast<float2 *>(ptrs[7]);
     D.counts = reinterpret_cast<int *>(ptrs[8]);
     D.start = reinterpret_cast<int *>(ptrs[9]);
-    D.tileSums = reinterpret_cast<int *>(ptrs[10]);
+    D.tileState = reinterpret_cast<unsigned long long *>(ptrs[10]);
     f.traw = reinterpret_cast<float2 *>(ptrs[11]);
     int *tkey = reinterpret_cast<int *>(ptrs[12]), *trank = reinterpret_cast<int *>(ptrs[13]);
     D.tpos = reinterpret_cast<float2 *>(ptrs[14]);
@@ -416,16 +416,19 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     D.by0 = 0.0f * f.slotCellSize - margin;
     D.bx1 = (float)f.slotsW * f.slotCellSize + margin;
     D.by1 = (float)f.slotsH * f.slotCellSize + margin;
-    f.sites = VmPointSet{D.gen, n, f.gridW, f.gridH, D.inv, D.key, D.rank, D.counts, D.start, D.tileSums,
+    f.sites = VmPointSet{D.gen, n, f.gridW, f.gridH, D.inv, D.key, D.rank, D.counts, D.start, nullptr,
                          D.sortedPos, D.sortedIdx, 1, 1};
-    f.tset = VmPointSet{f.traw, f.cap, f.gridW, f.gridH, D.inv, tkey, trank, D.counts, D.start, D.tileSums,
+    f.sites.tileState = D.tileState;
+    f.tset = VmPointSet{f.traw, f.cap, f.gridW, f.gridH, D.inv, tkey, trank, D.counts, D.start, nullptr,
                         D.tpos, D.tslot, 0, 1};
+    f.tset.tileState = D.tileState;
     cudaError_t e;
     if ((n && ((e = cudaMemcpyAsync(D.gen, in->generators, sizeof(float2) * n, cudaMemcpyHostToDevice, b->stream)) ||
                (e = cudaMemsetAsync(D.m, 0, 8 * (size_t)n, b->stream)) ||
                (e = cudaMemsetAsync(D.v, 0, 8 * (size_t)n, b->stream)) ||
                (e = cudaMemsetAsync(D.gradX, 0, 8 * kGradWords * (size_t)n, b->stream)))) ||
         (e = cudaMemsetAsync(D.counts, 0, 4 * ((size_t)f.cells + 1), b->stream)) ||
+        (e = cudaMemsetAsync(D.tileState, 0, 8 * ((size_t)f.tiles + 1), b->stream)) ||
         (e = cudaMemsetAsync(D.state, 0, sizeof(VmState), b->stream)) ||
         (e = cudaMemsetAsync(f.traw, 0xFF, 8 * (size_t)f.cap, b->stream)) ||
         (in->nTargets && (e = cudaMemcpyAsync(f.traw, in->targets, 8 * (size_t)in->nTargets, cudaMemcpyHostToDevice,
@@ -439,7 +442,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
     while (sub > 0 && ((long long)f.cells << (2 * sub)) > (1LL << 27)) --sub;
     long long keys = (long long)f.cells << (2 * sub);
     size_t tmpSizes[3] = {4 * (size_t)(keys + 1), 4 * (size_t)(keys + 1),
-                          4 * (size_t)((keys + kScanTile - 1) / kScanTile + 1)};
+                          8 * (size_t)((keys + kScanTile - 1) / kScanTile + 1)};
     size_t tmpOff[3];
     int nTmp = 0;
     if (sub > 0)
@@ -454,9 +457,10 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
         f.tset.sub = sub;
         f.tset.counts = reinterpret_cast<int *>(b->arena.base + tmpOff[0]);
         f.tset.start = reinterpret_cast<int *>(b->arena.base + tmpOff[1]);
-        f.tset.tileSums = reinterpret_cast<int *>(b->arena.base + tmpOff[2]);
+        f.tset.tileState = reinterpret_cast<unsigned long long *>(b->arena.base + tmpOff[2]);
         liveAt = f.tset.start + keys;
-        if ((e = cudaMemsetAsync(f.tset.counts, 0, tmpSizes[0], b->stream))) {
+        if ((e = cudaMemsetAsync(f.tset.counts, 0, tmpSizes[0], b->stream)) ||
+            (e = cudaMemsetAsync(f.tset.tileState, 0, tmpSizes[2], b->stream))) {
             releaseTmp();
             release_fit(b, f);
             return cuda_fail(e, "vmb_add_fit sort keys");

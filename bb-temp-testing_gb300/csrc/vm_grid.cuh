@@ -128,6 +128,109 @@ __device__ __forceinline__ void grid_tile_apply(const VmPointSet &S, int tile)
     if (tile == tiles - 1 && threadIdx.x == 0) S.start[cells] = offset + total;
 }
 
+// ---- two-pass scan with the tile prefixes made by the last tile -------------
+// Pass 1 stores each scan tile's sum in the set's tileState word and counts
+// the tile as done; the block that counts a set's last tile (every other
+// tile's sum is then written) turns the set's sums into exclusive prefixes and
+// writes start[cells]. Pass 2 scans each tile from its prefix. Nothing waits,
+// and each tile of pass 2 reads one prefix word instead of every earlier
+// tile's sum. tileState[tiles] (low half) is the set's done counter, zero
+// between scans.
+__device__ __forceinline__ int grid_tiles(const VmPointSet &S) { return (grid_keys(S) + kScanTile - 1) / kScanTile; }
+
+// The eight counts of this thread in the tile; `zero`: clear them for the next build.
+__device__ __forceinline__ void grid_load8(const VmPointSet &S, int base, int cells, int (&v)[8], bool zero)
+{
+    if (base + 8 <= cells) {
+        int4 *c = reinterpret_cast<int4 *>(S.counts + base);
+        int4 a = c[0], b = c[1];
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        if (zero) {
+            c[0] = make_int4(0, 0, 0, 0);
+            c[1] = make_int4(0, 0, 0, 0);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            v[k] = base + k < cells ? S.counts[base + k] : 0;
+            if (zero && base + k < cells) S.counts[base + k] = 0;
+        }
+    }
+}
+
+// Pass 1 for tile `tile` of S (256-thread block).
+__device__ __forceinline__ void grid_tile_reduce(const VmPointSet &S, int tile)
+{
+    __shared__ int red[24];
+    __shared__ int sLast;
+    int cells = grid_keys(S), tiles = grid_tiles(S);
+    int v[8];
+    grid_load8(S, tile * kScanTile + threadIdx.x * 8, cells, v, false);
+    int sum = v[0] + v[1] + v[2] + v[3] + v[4] + v[5] + v[6] + v[7];
+    sum = __reduce_add_sync(kFull, sum);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    unsigned *done = reinterpret_cast<unsigned *>(S.tileState + tiles);
+    if (threadIdx.x == 0) {
+        int t = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) t += red[w];
+        S.tileState[tile] = (unsigned)t;
+        __threadfence(); // the sum is visible before the tile counts as done
+        sLast = atomicAdd(done, 1u) == (unsigned)tiles - 1u;
+    }
+    __syncthreads();
+    if (!sLast) return;
+    // the set's last tile: exclusive prefixes of all its tiles' sums
+    __threadfence();
+    int carry = 0;
+    for (int b = 0; b < tiles; b += kScanTile) {
+        int w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int t = b + threadIdx.x * 8 + k;
+            w[k] = t < tiles ? (int)(unsigned)__ldcg(S.tileState + t) : 0;
+        }
+        int total;
+        int excl = block_scan8(w, red, total);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int t = b + threadIdx.x * 8 + k;
+            if (t < tiles) S.tileState[t] = (unsigned)(carry + excl + w[k]);
+        }
+        carry += total;
+        __syncthreads(); // red is reused by the next chunk
+    }
+    if (threadIdx.x == 0) {
+        S.start[cells] = carry;
+        *done = 0;
+    }
+}
+
+// Pass 2 for tile `tile` of S (256-thread block): start[] of its cells from
+// its prefix, counts zeroed again for the next build.
+__device__ __forceinline__ void grid_tile_scan(const VmPointSet &S, int tile)
+{
+    __shared__ int ws[24];
+    int cells = grid_keys(S);
+    int offset = (int)(unsigned)S.tileState[tile];
+    int base = tile * kScanTile + threadIdx.x * 8;
+    int v[8];
+    grid_load8(S, base, cells, v, true);
+    int total;
+    int at = offset + block_scan8(v, ws, total);
+    if (base + 8 <= cells) {
+        int4 *o = reinterpret_cast<int4 *>(S.start + base);
+        o[0] = make_int4(at + v[0], at + v[1], at + v[2], at + v[3]);
+        o[1] = make_int4(at + v[4], at + v[5], at + v[6], at + v[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (base + k < cells) S.start[base + k] = at + v[k];
+    }
+}
+
 // Cell-sorted copy of point i (its rank within the cell is the arrival order
 // of the binning atomics).
 __device__ __forceinline__ void grid_scatter_one(const VmPointSet &S, int i)

@@ -57,6 +57,18 @@ template <class T> struct DevBuf {
     int reserve(size_t count) { return count <= n && p ? VM_OK : alloc(count); }
 };
 
+// The tile words of a scan over `tiles` tiles (vm_launch_scan): allocated and
+// zeroed when too small, kept otherwise (every scan leaves the done counter zero).
+inline int zeroed_tile_state(DevBuf<unsigned long long> &b, int tiles, cudaStream_t s)
+{
+    size_t need = (size_t)tiles + 1;
+    if (b.p && b.n >= need) return VM_OK;
+    int rc = b.alloc(need);
+    if (rc) return rc;
+    cudaError_t e = cudaMemsetAsync(b.p, 0, need * sizeof(unsigned long long), s);
+    return e ? cuda_fail(e, "scan tile words") : VM_OK;
+}
+
 // The host part of the last Extract: the boundary (vertices, edges) and the
 // summary; the cells themselves stay on the device until copied out.
 struct MeshHost {

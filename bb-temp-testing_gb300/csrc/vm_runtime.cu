@@ -106,7 +106,7 @@ struct vm_optimizer {
 
     DevBuf<float2> gen, m, v, sortedPos, traw, tpos, stageVals, qbuf, cellVerts;
     DevBuf<long long> gradX;
-    DevBuf<int> key, rank, counts, start, tileSums, sortedIdx, tkey, trank, tslot, stageSlots, kIdx, cellEdges,
+    DevBuf<int> key, rank, counts, start, sortedIdx, tkey, trank, tslot, stageSlots, kIdx, cellEdges,
         cellCount, flags, dbgI0, dbgJ;
     DevBuf<float> kD2, dbgLoss;
     DevBuf<unsigned char> inside;
@@ -114,7 +114,8 @@ struct vm_optimizer {
     DevBuf<VmState> state;
     DevBuf<VmFit> dFit;
     DevBuf<VmPointSet> dSites, dTargets, dCsrSet;
-    DevBuf<int> cellStartD, csrTiles, csrLabels, dCsrPre; // extraction: cells packed in CSR order
+    DevBuf<int> cellStartD, csrLabels, dCsrPre; // extraction: cells packed in CSR order
+    DevBuf<unsigned long long> tileState, ttileState, csrTileState; // scan tile words (vm_launch_scan)
     DevBuf<int> bndCnt, bndPartial, bndErr, bndMin, bndFirst, bndEdges; // boundary assembly
     DevBuf<unsigned long long> bndKeys;
     DevBuf<unsigned> bndSlot;
@@ -124,7 +125,7 @@ struct vm_optimizer {
     DevBuf<float2> csrVerts;
     DevBuf<int> dPre; // [0, siteBlocks, 0, tiles, 0, lossTiles, 0, targetBlocks]
     DevBuf<int> dTPre; // [0, targetBlocks, 0, targetKeyTiles]
-    DevBuf<int> tcounts, tstart, ttileSums; // target sort by sub-cell (only while sorting)
+    DevBuf<int> tcounts, tstart; // target sort by sub-cell (only while sorting)
     DevBuf<char> queue;  // deferred-target queue header
     DevBuf<int2> qitems; // its items
     std::vector<cudaEvent_t> timing; // vm_step_timed events
@@ -163,13 +164,13 @@ int upload_tables(vm_optimizer *h)
     F.active = 1;
     F.fastShift = vm_fast_shift(h->block5Max);
     F.gen = h->gen.p; F.m = h->m.p; F.v = h->v.p; F.gradX = h->gradX.p;
-    F.key = h->key.p; F.rank = h->rank.p; F.counts = h->counts.p; F.start = h->start.p; F.tileSums = h->tileSums.p;
+    F.key = h->key.p; F.rank = h->rank.p; F.counts = h->counts.p; F.start = h->start.p; F.tileState = h->tileState.p;
     F.sortedIdx = h->sortedIdx.p; F.sortedPos = h->sortedPos.p;
     F.tpos = h->tpos.p; F.tslot = h->tslot.p;
     F.state = h->state.p;
     VmPointSet S{};
     S.pts = h->gen.p; S.n = n; S.gridW = h->gridW; S.gridH = h->gridH; S.inv = F.inv;
-    S.key = h->key.p; S.rank = h->rank.p; S.counts = h->counts.p; S.start = h->start.p; S.tileSums = h->tileSums.p;
+    S.key = h->key.p; S.rank = h->rank.p; S.counts = h->counts.p; S.start = h->start.p; S.tileState = h->tileState.p;
     S.outPos = h->sortedPos.p; S.outIdx = h->sortedIdx.p; S.canonical = 1; S.useIndexOrder = 1;
     int pre[8] = {0, (n + 255) / 256, 0, h->tiles, 0, (h->liveTargets + h->lossTile - 1) / h->lossTile, 0,
                   (h->targetCapacity + 255) / 256};
@@ -382,12 +383,12 @@ int sort_targets(vm_optimizer *h)
     int keyTiles = (int)((keys + kScanTile - 1) / kScanTile);
     int tb = (h->targetCapacity + 255) / 256;
     if ((rc = h->tcounts.alloc(keys + 1)) || (rc = h->tstart.alloc(keys + 1)) ||
-        (rc = h->ttileSums.alloc(keyTiles + 1)))
+        (rc = zeroed_tile_state(h->ttileState, keyTiles, h->stream)))
         return rc;
     VmPointSet T{};
     T.pts = h->traw.p; T.n = h->targetCapacity; T.gridW = h->gridW; T.gridH = h->gridH; T.inv = 1.0f / h->spacing;
     T.key = h->tkey.p; T.rank = h->trank.p; T.counts = h->tcounts.p; T.start = h->tstart.p;
-    T.tileSums = h->ttileSums.p; T.outPos = h->tpos.p; T.outIdx = h->tslot.p; T.canonical = 0; T.useIndexOrder = 1;
+    T.tileState = h->ttileState.p; T.outPos = h->tpos.p; T.outIdx = h->tslot.p; T.canonical = 0; T.useIndexOrder = 1;
     T.sub = sub;
     int pre[4] = {0, tb, 0, keyTiles};
     if ((e = cudaMemsetAsync(h->tcounts.p, 0, sizeof(int) * (size_t)(keys + 1), h->stream)) ||
@@ -409,7 +410,7 @@ int sort_targets(vm_optimizer *h)
     if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "target sort");
     h->tcounts.release();
     h->tstart.release();
-    h->ttileSums.release();
+    h->ttileState.release();
     if (live != h->liveTargets) drop_graph(h);
     h->liveTargets = live;
     h->block5Max = b5;
@@ -505,7 +506,7 @@ int vm_create(float width, float height, float spacing, const vm_params *params,
         rc = cuda_fail(e, "stream/event");
     if (!rc) rc = h->counts.alloc(h->cells + 1);
     if (!rc) rc = h->start.alloc(h->cells + 1);
-    if (!rc) rc = h->tileSums.alloc(h->tiles + 1);
+    if (!rc) rc = zeroed_tile_state(h->tileState, h->tiles, h->stream);
     if (!rc) rc = h->state.alloc(1);
     if (!rc) rc = h->dFit.alloc(1);
     if (!rc) rc = h->dSites.alloc(1);
@@ -1026,11 +1027,11 @@ int vm_extract(vm_optimizer *h, vm_mesh_info *info)
     C.gridH = 1;
     C.counts = h->cellCount.p;
     int pre[2] = {0, tiles};
-    if ((rc = h->cellStartD.reserve((size_t)n + 1)) || (rc = h->csrTiles.reserve((size_t)tiles + 1)) ||
+    if ((rc = h->cellStartD.reserve((size_t)n + 1)) || (rc = zeroed_tile_state(h->csrTileState, tiles, h->stream)) ||
         (rc = h->dCsrSet.reserve(1)) || (rc = h->dCsrPre.reserve(2)))
         return rc;
     C.start = h->cellStartD.p;
-    C.tileSums = h->csrTiles.p;
+    C.tileState = h->csrTileState.p;
     int total = 0, flags[2], nBnd = 0, nVert = 0;
     if ((e = cudaMemcpyAsync(h->dCsrSet.p, &C, sizeof(C), cudaMemcpyHostToDevice, h->stream)) ||
         (e = cudaMemcpyAsync(h->dCsrPre.p, pre, sizeof(pre), cudaMemcpyHostToDevice, h->stream)) ||

@@ -1,8 +1,9 @@
 // VoroMesh optimisation step kernels (batch-native).
 //
 //   k_bin          cell key + atomic count per point        (reference binKernel, voro_optimizer.cu:168-177)
-//   k_scan_tiles   per-tile sums of the cell counts          (reference cub ExclusiveSum, :697)
-//   k_scan_apply   exclusive scan -> cell start
+//   k_scan_tiles   per-tile sums of the cell counts; a set's last tile turns
+//                  them into tile prefixes           (reference cub ExclusiveSum, :697)
+//   k_scan_apply   exclusive scan of each tile from its prefix -> cell start
 //   k_scatter      cell-sorted copy (reference scatterKernel :179-187)
 //   k_canonical    each cell's run sorted by slot index (before the grid is exported)
 //   (k_loss        VoroLoss + analytic gradient per target, vm_loss.cu)
@@ -12,10 +13,10 @@
 //   k_finalize     publish a loss-only pass (EvaluateLoss, :746-761)
 //   k_knn          exact kNN query operator (reference knn<K>, :130-163)
 //
-// One step of a set of fits is: k_loss -> k_adam_bin -> k_scan_tiles ->
-// k_scan_apply -> k_scatter(publish). The grid is therefore always built for
-// the current generators between steps, as the reference rebuilds it at the
-// start of each step. Nothing in the step depends on the order within a
+// One step of a set of fits is: k_loss -> k_loss_exact -> k_adam_bin ->
+// k_scan_tiles -> k_scan_apply -> k_scatter(publish). The grid is therefore
+// always built for the current generators between steps, as the reference
+// rebuilds it at the start of each step. Nothing in the step depends on the order within a
 // cell's run (every argmin breaks ties by index, every sum is exact), so
 // k_canonical runs only before the grid is exported.
 #include "vm_device.cuh"
@@ -24,6 +25,14 @@
 #include "vm_kernels.h"
 
 namespace vmk {
+
+// The scatter keeps the 256-site block of the site prefix tables but serves it
+// with 64 threads, four sites each: their loads are issued together and the
+// whole launch fits on the GPU at once, so each thread's chain of dependent
+// loads (key, then the cell's start) is paid once.
+constexpr int kSiteBlock = 256;
+constexpr int kSiteThreads = 64;
+constexpr int kSitesPerThread = kSiteBlock / kSiteThreads;
 
 // ---------------------------------------------------------------------------
 // hash grid build over a table of point sets (bodies in vm_grid.cuh)
@@ -35,18 +44,21 @@ __global__ void __launch_bounds__(256) k_bin(const VmPointSet *__restrict__ sets
     grid_bin_one(sets[f], (blockIdx.x - prefix[f]) * blockDim.x + threadIdx.x, emptyIsNegative);
 }
 
+// The scan of the cell counts, one block per scan tile of every set (bodies
+// in vm_grid.cuh): tile sums, with each set's tile prefixes made by its last
+// tile; then each tile's cells.
 __global__ void __launch_bounds__(256) k_scan_tiles(const VmPointSet *__restrict__ sets,
                                                     const int *__restrict__ prefix, int nSets)
 {
     int f = find_fit(prefix, nSets, blockIdx.x);
-    grid_tile_sum(sets[f], blockIdx.x - prefix[f]);
+    grid_tile_reduce(sets[f], blockIdx.x - prefix[f]);
 }
 
 __global__ void __launch_bounds__(256) k_scan_apply(const VmPointSet *__restrict__ sets,
                                                     const int *__restrict__ prefix, int nSets)
 {
     int f = find_fit(prefix, nSets, blockIdx.x);
-    grid_tile_apply(sets[f], blockIdx.x - prefix[f]);
+    grid_tile_scan(sets[f], blockIdx.x - prefix[f]);
 }
 
 __global__ void __launch_bounds__(256) k_canonical(const VmPointSet *__restrict__ sets,
@@ -58,8 +70,9 @@ __global__ void __launch_bounds__(256) k_canonical(const VmPointSet *__restrict_
     if (sets[f].canonical) grid_canonical_one(sets[f], (blockIdx.x - prefix[f] * kPer) * 256 + threadIdx.x);
 }
 
-__global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ sets, const int *__restrict__ prefix,
-                                                 int nSets, const VmFit *__restrict__ publish)
+__global__ void __launch_bounds__(kSiteThreads) k_scatter(const VmPointSet *__restrict__ sets,
+                                                          const int *__restrict__ prefix, int nSets,
+                                                          const VmFit *__restrict__ publish)
 {
     int f = find_fit(prefix, nSets, blockIdx.x);
     int local = blockIdx.x - prefix[f];
@@ -75,7 +88,32 @@ __global__ void __launch_bounds__(256) k_scatter(const VmPointSet *__restrict__ 
         st->needExact = 0;
         st->dUsed = 0;
     }
-    grid_scatter_one(sets[f], local * blockDim.x + threadIdx.x);
+    // the block's points (grid_scatter_one, several per thread with their
+    // loads issued together)
+    const VmPointSet &S = sets[f];
+    int i0 = local * kSiteBlock + threadIdx.x;
+    int c[kSitesPerThread], r[kSitesPerThread];
+    float2 q[kSitesPerThread];
+#pragma unroll
+    for (int k = 0; k < kSitesPerThread; ++k) {
+        int i = i0 + k * kSiteThreads;
+        c[k] = -1;
+        if (i < S.n) {
+            c[k] = S.key[i];
+            r[k] = S.rank[i];
+            q[k] = S.pts[i];
+        }
+    }
+    int at[kSitesPerThread];
+#pragma unroll
+    for (int k = 0; k < kSitesPerThread; ++k)
+        if (c[k] >= 0) at[k] = S.start[c[k]] + r[k];
+#pragma unroll
+    for (int k = 0; k < kSitesPerThread; ++k)
+        if (c[k] >= 0) {
+            S.outIdx[at[k]] = i0 + k * kSiteThreads;
+            S.outPos[at[k]] = q[k];
+        }
 }
 
 // Publishes a loss-only pass: loss and count of the accumulator, iteration kept.
@@ -249,7 +287,7 @@ cudaError_t vm_launch_scatter(const VmPointSet *sets, const int *prefix, int nSe
                               const VmFit *publish, cudaStream_t s)
 {
     if (totalBlocks <= 0) return cudaSuccess;
-    k_scatter<<<totalBlocks, 256, 0, s>>>(sets, prefix, nSets, publish);
+    k_scatter<<<totalBlocks, kSiteThreads, 0, s>>>(sets, prefix, nSets, publish);
     return cudaGetLastError();
 }
 

@@ -62,7 +62,7 @@ struct VmFit {
     int *key, *rank;      // per slot: grid cell (-1 empty) and rank within the cell
     int *counts;          // gridW*gridH (+1): per-cell counts, zero between builds
     int *start;           // gridW*gridH + 1: cell start in the sorted arrays
-    int *tileSums;        // per scan tile
+    unsigned long long *tileState; // the site grid's scan words (VmPointSet::tileState)
     int *sortedIdx;       // live slots in cell order, ascending slot within a cell
     VM_F2 *sortedPos;
     VM_F2 *tpos;          // live targets in cell order
@@ -85,6 +85,10 @@ struct VmPointSet {
     int canonical; // sort each cell's run by index after the scatter
     int useIndexOrder; // outIdx holds the source index (always 1 today)
     int sub;           // log2 of the sub-cells per cell side in the sort key (targets; 0 for sites)
+    // The scan of vm_launch_scan: one word per scan tile (its sum, then its
+    // prefix) and a done counter after them, zero between scans. tileSums
+    // serves the allocation-free build's scan only.
+    unsigned long long *tileState;
 };
 
 constexpr int kScanTile = 2048; // cells per scan tile (256 threads x 8)
