@@ -16,9 +16,9 @@
 // One step of a set of fits is: k_loss -> k_loss_exact -> k_adam_bin ->
 // k_scan_tiles -> k_scan_apply -> k_scatter(publish). The grid is therefore
 // always built for the current generators between steps, as the reference
-// rebuilds it at the start of each step. Nothing in the step depends on the order within a
-// cell's run (every argmin breaks ties by index, every sum is exact), so
-// k_canonical runs only before the grid is exported.
+// rebuilds it at the start of each step. Nothing in the step depends on the
+// order within a cell's run (every argmin breaks ties by index, every sum is
+// exact), so k_canonical runs only before the grid is exported.
 #include "vm_device.cuh"
 #include "vm_grid.cuh"
 #include "vm_knn.cuh"
@@ -182,19 +182,34 @@ __global__ void __launch_bounds__(256) k_adam_bin(const VmFit *__restrict__ fits
     }
     if (p.x >= 0.0f && inRegion) {
         float2 m = F.m[i], v = F.v[i];
-        float b1 = F.beta1, b2 = F.beta2;
-        float mx = b1 * m.x + (1.0f - b1) * grx;
-        float my = b1 * m.y + (1.0f - b1) * gry;
-        float vx = b2 * v.x + (1.0f - b2) * (grx * grx);
-        float vy = b2 * v.y + (1.0f - b2) * (gry * gry);
-        F.m[i] = make_float2(mx, my);
-        F.v[i] = make_float2(vx, vy);
-        float eps = F.eps;
-        p.x -= lr * (mx / bc1) / (sqrtf(vx / bc2) + eps);
-        p.y -= lr * (my / bc1) / (sqrtf(vy / bc2) + eps);
-        p.x = fminf(fmaxf(p.x, 0.0f), F.width);
-        p.y = fminf(fmaxf(p.y, 0.0f), F.height);
-        F.gen[i] = p;
+        float b1 = F.beta1, b2 = F.beta2, eps = F.eps;
+        // A slot with a zero gradient and zero moments: the update keeps the
+        // moments at +0 and subtracts +0 from p (+0 / bc1 = +0, sqrtf(+0) + eps
+        // = eps, lr * +0 / eps = +0, p - +0 = p for every p), so only the clamp
+        // acts. Exact for lr, bc1, bc2, eps > 0 and finite beta1, beta2
+        // (checked); the slots far from every target take this path.
+        bool idle = (__float_as_uint(grx) | __float_as_uint(gry) | __float_as_uint(m.x) | __float_as_uint(m.y) |
+                     __float_as_uint(v.x) | __float_as_uint(v.y)) == 0u &&
+                    lr > 0.0f && lr < FLT_MAX && bc1 > 0.0f && bc2 > 0.0f && eps > 0.0f && fabsf(b1) < FLT_MAX &&
+                    fabsf(b2) < FLT_MAX;
+        if (idle) {
+            float2 q = make_float2(fminf(fmaxf(p.x, 0.0f), F.width), fminf(fmaxf(p.y, 0.0f), F.height));
+            if (__float_as_uint(q.x) != __float_as_uint(p.x) || __float_as_uint(q.y) != __float_as_uint(p.y))
+                F.gen[i] = q;
+            p = q;
+        } else {
+            float mx = b1 * m.x + (1.0f - b1) * grx;
+            float my = b1 * m.y + (1.0f - b1) * gry;
+            float vx = b2 * v.x + (1.0f - b2) * (grx * grx);
+            float vy = b2 * v.y + (1.0f - b2) * (gry * gry);
+            F.m[i] = make_float2(mx, my);
+            F.v[i] = make_float2(vx, vy);
+            p.x -= lr * (mx / bc1) / (sqrtf(vx / bc2) + eps);
+            p.y -= lr * (my / bc1) / (sqrtf(vy / bc2) + eps);
+            p.x = fminf(fmaxf(p.x, 0.0f), F.width);
+            p.y = fminf(fmaxf(p.y, 0.0f), F.height);
+            F.gen[i] = p;
+        }
     }
     if (p.x < 0.0f) {
         F.key[i] = -1;
