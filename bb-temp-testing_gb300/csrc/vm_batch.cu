@@ -198,7 +198,7 @@ int enqueue_batch_step(vmb_batch *b)
     if (!nf) return VM_OK;
     int *sitePre = b->dPre.p, *scanPre = b->dPre.p + (nf + 1), *lossPre = b->dPre.p + 2 * (nf + 1);
     cudaError_t e;
-    if ((e = vm_launch_loss(b->dFits.p, lossPre, nf, b->lossTiles, 0, b->lossGrid, b->lossVariant, b->queue.p,
+    if ((e = vm_launch_loss(b->dFits.p, lossPre, nf, b->lossTiles, 0, b->lossGrid, b->lossVariant, 0, b->queue.p,
                             b->stream)) ||
         (e = vm_launch_adam_bin(b->dFits.p, sitePre, nf, b->siteBlocks, b->queue.p, b->stream)) ||
         (e = vm_launch_scan(b->dSites.p, scanPre, nf, b->scanTiles, b->stream)) ||
@@ -550,7 +550,7 @@ int vmb_evaluate(vmb_batch *b, float *losses)
     if (nf) {
         cudaError_t e;
         if ((e = vm_launch_loss(b->dFits.p, b->dPre.p + 2 * (nf + 1), nf, b->lossTiles, 1, b->lossGrid,
-                                b->lossVariant, b->queue.p, b->stream)) ||
+                                b->lossVariant, 0, b->queue.p, b->stream)) ||
             (e = vm_launch_finalize(b->dFits.p, nf, b->queue.p, b->stream)))
             return cuda_fail(e, "batch evaluate");
     }

@@ -22,9 +22,19 @@ cudaError_t vm_launch_canonical(const VmPointSet *sets, const int *tilePrefix, i
 // targets, then the exact ring search over the targets it deferred to the
 // queue (created by vm_queue_init; items hold (fit, target) int2 pairs).
 // `variant` picks block size and occupancy target; its block size is also the
-// number of targets per tile the prefix table counts.
+// number of targets per tile the prefix table counts. With `windowed`, every
+// fit has a window list (VmFit::twin) and a tile is block size / 32 windows.
 cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode,
-                           int gridBlocks, int variant, void *queue, cudaStream_t s);
+                           int gridBlocks, int variant, int windowed, void *queue, cudaStream_t s);
+// The loss windows of a fit's cell-sorted targets (VmFit::twin): each grid
+// cell's run split into windows of at most 32. tstart holds the target sort's
+// key starts (cells << 2 sub keys); winSet is a device VmPointSet over `cells`
+// keys (counts, start, tileState of tiles + 1 words) and winPre its tile
+// prefix {0, tiles}; twin needs room for start[cells] + 1 entries, at most
+// live / 32 + min(cells, live) + 1.
+cudaError_t vm_launch_target_windows(const int *tstart, int cells, int sub, const VmPointSet *winSet,
+                                     const int *winPre, int tiles, int *counts, const int *start, int *twin,
+                                     cudaStream_t s);
 int vm_loss_variants();
 int vm_loss_variant_threads(int variant);
 cudaError_t vm_launch_finalize(const VmFit *fits, int nFits, void *queue, cudaStream_t s);

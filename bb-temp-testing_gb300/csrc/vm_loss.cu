@@ -587,15 +587,19 @@ __device__ __forceinline__ void flag_fit(const VmFit &F, int f, SlowQueue *queue
     }
 }
 
-// One block takes a contiguous range of tiles (THREADS targets each) of the
-// fit-concatenated target order; within each fit's part of it, every warp
-// walks its own contiguous run of targets, 32 per iteration. The lanes of an
-// iteration are served in groups that share a grid cell (normally one group):
+// One block takes a contiguous range of tiles (THREADS targets, or with WIN
+// THREADS / 32 windows, each) of the fits' concatenated target order; within
+// each fit's part of it, every warp walks
+// its own contiguous run of windows, one per iteration. A window is 32
+// targets in target order, or, with WIN (fits with a window list: small fits,
+// whose pass is as long as its slowest warp), a cell-aligned run of at most
+// 32. The lanes of an iteration are served in groups that share a grid cell
+// (normally one group; always one with cell-aligned windows):
 // the 5x5 cell block around the group's cell is staged once in shared memory
 // (and kept while the warp stays in that cell), and distance bounds to the
 // group's bounding box cut the candidates of both passes of loss_staged to
 // the few sites some lane can need.
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, bool WIN>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_loss(const VmFit *__restrict__ fits, const int *__restrict__ prefix, int nFits, int mode, SlowQueue *queue)
 {
@@ -620,19 +624,33 @@ __global__ void __launch_bounds__(THREADS, MINB)
         load_fit(fits, f, sF, sIter);
         long long segEnd = min(t1, (long long)prefix[f + 1]);
         bool active = F.active || mode == 1;
-        // this fit's targets in the block's range, then this warp's run of them
-        int A = (int)(t - prefix[f]) * THREADS;
-        int B = min((int)(segEnd - prefix[f]) * THREADS, F.nTargets);
-        int per = B > A ? (B - A + NW * 32 - 1) / (NW * 32) * 32 : 0;
-        int w0 = A + warp * per, w1 = min(w0 + per, B);
+        // this fit's part of the block's range, then this warp's run of it:
+        // targets (32 an iteration), or with WIN windows (one an iteration; a
+        // tile is NW windows)
+        int w0, w1;
+        if constexpr (WIN) {
+            int A = (int)(t - prefix[f]) * NW;
+            int B = min((int)(segEnd - prefix[f]) * NW, F.nWindows);
+            int per = B > A ? (B - A + NW - 1) / NW : 0;
+            w0 = A + warp * per;
+            w1 = min(w0 + per, B);
+        } else {
+            int A = (int)(t - prefix[f]) * THREADS;
+            int B = min((int)(segEnd - prefix[f]) * THREADS, F.nTargets);
+            int per = B > A ? (B - A + NW * 32 - 1) / (NW * 32) * 32 : 0;
+            w0 = A + warp * per;
+            w1 = min(w0 + per, B);
+        }
         if (!active) w1 = w0;
         unsigned long long aLo = 0, aHi = 0;
         int aCnt = 0, aSlow = 0;
         unsigned long long *G = reinterpret_cast<unsigned long long *>(F.gradX);
         RunSum run0, runJ;
-        for (int base = w0; base < w1; base += 32) {
+        for (int it = w0; it < w1; it += WIN ? 1 : 32) {
+            int base = WIN ? F.twin[it] : it;
+            int end = WIN ? F.twin[it + 1] : w1;
             int local = base + lane;
-            bool valid = local < w1;
+            bool valid = local < end;
             float2 p = make_float2(0.0f, 0.0f);
             bool take = false;
             int cx = 0, cy = 0;
@@ -836,32 +854,35 @@ constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 int vm_loss_variants() { return kNumVariants; }
 int vm_loss_variant_threads(int v) { return kVariants[v < 0 || v >= kNumVariants ? 0 : v].threads; }
 
-template <int T, int B> static void *loss_fn() { return (void *)k_loss<T, B>; }
+template <int T, int B> static void *loss_fn(bool win)
+{
+    return win ? (void *)k_loss<T, B, true> : (void *)k_loss<T, B, false>;
+}
 
-static void *variant_fn(int v)
+static void *variant_fn(int v, bool win)
 {
     switch (v) {
-    case 0: return loss_fn<256, 4>();
-    case 1: return loss_fn<256, 3>();
-    case 2: return loss_fn<256, 2>();
-    case 3: return loss_fn<128, 5>();
-    case 4: return loss_fn<128, 6>();
-    case 5: return loss_fn<64, 16>();
-    case 6: return loss_fn<64, 12>();
-    default: return loss_fn<64, 10>();
+    case 0: return loss_fn<256, 4>(win);
+    case 1: return loss_fn<256, 3>(win);
+    case 2: return loss_fn<256, 2>(win);
+    case 3: return loss_fn<128, 5>(win);
+    case 4: return loss_fn<128, 6>(win);
+    case 5: return loss_fn<64, 16>(win);
+    case 6: return loss_fn<64, 12>(win);
+    default: return loss_fn<64, 10>(win);
     }
 }
 
 cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int mode,
-                           int gridBlocks, int variant, void *queue, cudaStream_t s)
+                           int gridBlocks, int variant, int windowed, void *queue, cudaStream_t s)
 {
     SlowQueue *q = static_cast<SlowQueue *>(queue);
     if (totalTiles > 0) {
         int g = gridBlocks < totalTiles ? gridBlocks : totalTiles;
         if (g < 1) g = 1;
         void *args[] = {(void *)&fits, (void *)&tilePrefix, (void *)&nFits, (void *)&mode, (void *)&q};
-        cudaError_t e =
-            cudaLaunchKernel(variant_fn(variant), dim3(g), dim3(vm_loss_variant_threads(variant)), args, 0, s);
+        cudaError_t e = cudaLaunchKernel(variant_fn(variant, windowed != 0), dim3(g),
+                                         dim3(vm_loss_variant_threads(variant)), args, 0, s);
         if (e) return e;
     }
     // with no targets the step still needs its Adam schedule (k_loss_exact)
@@ -877,7 +898,7 @@ int vm_loss_occupancy_blocks(int variant)
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, variant_fn(variant), vm_loss_variant_threads(variant), 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, variant_fn(variant, false), vm_loss_variant_threads(variant), 0);
     if (per < 1) per = 1;
     return sms * per;
 }

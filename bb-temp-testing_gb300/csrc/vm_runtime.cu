@@ -136,11 +136,31 @@ struct vm_optimizer {
     long long exactTotal = 0;
     int block5Max = 0;          // most live targets in any 5x5 block of cells (sets the split shift)
     DevBuf<int> block5Buf;
+    // the loss windows of a small fit (nWindows > 0): cell-aligned runs of at
+    // most 32 targets (vm_launch_target_windows)
+    int nWindows = 0;
+    DevBuf<int> twin;
+    DevBuf<int> winCounts, winStart; // the window counts and their scan
+    DevBuf<unsigned long long> winState;
+    DevBuf<VmPointSet> dWinSet;
+    DevBuf<int> dWinPre;
+    int winPre[2] = {0, 0}; // host copy of dWinPre (read by an async copy)
 
     int numSlots() const { return slotsW * slotsH; }
 };
 
 namespace {
+
+// Loss tiles of the fit: targets per tile = the variant's block size, or with
+// a window list block size / 32 windows per tile.
+int loss_tiles(const vm_optimizer *h)
+{
+    if (h->nWindows > 0) {
+        int nw = h->lossTile / 32;
+        return (h->nWindows + nw - 1) / nw;
+    }
+    return (h->liveTargets + h->lossTile - 1) / h->lossTile;
+}
 
 int upload_tables(vm_optimizer *h)
 {
@@ -163,6 +183,8 @@ int upload_tables(vm_optimizer *h)
     F.nTargets = h->liveTargets;
     F.active = 1;
     F.fastShift = vm_fast_shift(h->block5Max);
+    F.twin = h->nWindows > 0 ? h->twin.p : nullptr;
+    F.nWindows = h->nWindows;
     F.gen = h->gen.p; F.m = h->m.p; F.v = h->v.p; F.gradX = h->gradX.p;
     F.key = h->key.p; F.rank = h->rank.p; F.counts = h->counts.p; F.start = h->start.p; F.tileState = h->tileState.p;
     F.sortedIdx = h->sortedIdx.p; F.sortedPos = h->sortedPos.p;
@@ -172,8 +194,7 @@ int upload_tables(vm_optimizer *h)
     S.pts = h->gen.p; S.n = n; S.gridW = h->gridW; S.gridH = h->gridH; S.inv = F.inv;
     S.key = h->key.p; S.rank = h->rank.p; S.counts = h->counts.p; S.start = h->start.p; S.tileState = h->tileState.p;
     S.outPos = h->sortedPos.p; S.outIdx = h->sortedIdx.p; S.canonical = 1; S.useIndexOrder = 1;
-    int pre[8] = {0, (n + 255) / 256, 0, h->tiles, 0, (h->liveTargets + h->lossTile - 1) / h->lossTile, 0,
-                  (h->targetCapacity + 255) / 256};
+    int pre[8] = {0, (n + 255) / 256, 0, h->tiles, 0, loss_tiles(h), 0, (h->targetCapacity + 255) / 256};
     cudaError_t e;
     if ((e = cudaMemcpyAsync(h->dFit.p, &F, sizeof(VmFit), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload fit");
     if ((e = cudaMemcpyAsync(h->dSites.p, &S, sizeof(S), cudaMemcpyHostToDevice, h->stream))) return cuda_fail(e, "upload sites");
@@ -259,11 +280,12 @@ int autotune_loss_variant(vm_optimizer *h)
         for (int v = 0; v < nv; ++v) {
             set_loss_variant(h, v);
             if ((rc = upload_tables(h))) return rc;
-            int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
+            int lossTiles = loss_tiles(h);
             float ms = 0.0f;
             for (int k = 0; k < 6; ++k) {
                 if (k == 1 && (e = cudaEventRecord(h->ev0, h->stream))) return cuda_fail(e, "tune event");
-                if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, v, h->queue.p,
+                if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, v, h->nWindows > 0,
+                                        h->queue.p,
                                         h->stream)) ||
                     (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream)))
                     return cuda_fail(e, "tune pass");
@@ -311,8 +333,9 @@ int enqueue_step(vm_optimizer *h)
 {
     int n = h->numSlots();
     cudaError_t e;
-    int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
-    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, h->lossVariant, h->queue.p, h->stream)))
+    int lossTiles = loss_tiles(h);
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, h->lossVariant, h->nWindows > 0,
+                            h->queue.p, h->stream)))
         return cuda_fail(e, "loss");
     if ((e = vm_launch_adam_bin(h->dFit.p, h->dPre.p + 0, 1, (n + 255) / 256, h->queue.p, h->stream)))
         return cuda_fail(e, "adam");
@@ -372,6 +395,43 @@ int target_sub(const vm_optimizer *h)
     return sub;
 }
 
+// A fit with fewer live targets than this is latency-bound: its loss pass
+// lasts as long as its slowest warp, so it gets cell-aligned windows (one grid
+// cell per warp iteration, instead of up to three for 32 consecutive targets).
+// Larger fits are throughput-bound and keep windows of 32 targets, which
+// need fewer iterations.
+constexpr int kWindowedTargets = 1 << 19;
+
+// Enqueues the loss windows of the sorted targets (vm_launch_target_windows)
+// for at most `live` live targets, from the target sort's key starts
+// (h->tstart); their number lands in *nWin once the stream has reached it.
+int enqueue_windows(vm_optimizer *h, int sub, int live, int *nWin)
+{
+    int cells = h->cells, tiles = (cells + kScanTile - 1) / kScanTile;
+    int rc;
+    if ((rc = h->winCounts.reserve((size_t)cells + 1)) || (rc = h->winStart.reserve((size_t)cells + 1)) ||
+        (rc = zeroed_tile_state(h->winState, tiles, h->stream)) ||
+        (rc = h->twin.reserve((size_t)live / 32 + std::min(cells, live) + 1)) || (rc = h->dWinSet.reserve(1)) ||
+        (rc = h->dWinPre.reserve(2)))
+        return rc;
+    VmPointSet W{};
+    W.gridW = cells;
+    W.gridH = 1;
+    W.counts = h->winCounts.p;
+    W.start = h->winStart.p;
+    W.tileState = h->winState.p;
+    h->winPre[0] = 0;
+    h->winPre[1] = tiles;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(h->dWinSet.p, &W, sizeof(W), cudaMemcpyHostToDevice, h->stream)) ||
+        (e = cudaMemcpyAsync(h->dWinPre.p, h->winPre, sizeof(h->winPre), cudaMemcpyHostToDevice, h->stream)) ||
+        (e = vm_launch_target_windows(h->tstart.p, cells, sub, h->dWinSet.p, h->dWinPre.p, tiles, h->winCounts.p,
+                                      h->winStart.p, h->twin.p, h->stream)) ||
+        (e = cudaMemcpyAsync(nWin, h->winStart.p + cells, sizeof(int), cudaMemcpyDeviceToHost, h->stream)))
+        return cuda_fail(e, "loss windows");
+    return VM_OK;
+}
+
 // Targets in (cell, sub-cell) order, the order the loss pass walks them. The
 // key arrays exist only during the sort.
 int sort_targets(vm_optimizer *h)
@@ -406,13 +466,24 @@ int sort_targets(vm_optimizer *h)
     if ((e = cudaMemcpyAsync(&live, h->tstart.p + keys, sizeof(int), cudaMemcpyDeviceToHost, h->stream)) ||
         (e = cudaMemcpyAsync(&b5, h->block5Buf.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream)))
         return cuda_fail(e, "live targets");
+    // a small fit's loss windows, in the same pass when every target slot
+    // would still make it a small fit
+    int nWin = 0;
+    bool windowsQueued = h->targetCapacity < kWindowedTargets;
+    if (windowsQueued && (rc = enqueue_windows(h, sub, h->targetCapacity, &nWin))) return rc;
     // the tables above live on the host stack
     if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "target sort");
+    if (live > 0 && live < kWindowedTargets && !windowsQueued) {
+        if ((rc = enqueue_windows(h, sub, live, &nWin))) return rc;
+        if ((e = cudaStreamSynchronize(h->stream))) return cuda_fail(e, "loss windows");
+    }
+    if (!(live > 0 && live < kWindowedTargets)) nWin = 0;
     h->tcounts.release();
     h->tstart.release();
     h->ttileState.release();
-    if (live != h->liveTargets) drop_graph(h);
+    if (live != h->liveTargets || nWin != h->nWindows) drop_graph(h);
     h->liveTargets = live;
+    h->nWindows = nWin;
     h->block5Max = b5;
     int qcap = std::max(live, 1); // every live target fits: the loss never overflows the queue
     int sms = 0, dev = 0;
@@ -773,12 +844,13 @@ int vm_step_timed(vm_optimizer *h, int iterations, float *stageMs)
         h->timing.push_back(ev);
     }
     int n = h->numSlots();
-    int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
+    int lossTiles = loss_tiles(h);
     h->gridCanonical = false; // the steps rebuild the grid
     for (int k = 0; k < iterations; ++k) {
         cudaEvent_t *ev = &h->timing[(size_t)k * 5];
         if ((e = cudaEventRecord(ev[0], h->stream)) ||
-            (e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+            (e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, h->lossVariant,
+                                h->nWindows > 0, h->queue.p, h->stream)) ||
             (e = cudaEventRecord(ev[1], h->stream)) ||
             (e = vm_launch_adam_bin(h->dFit.p, h->dPre.p + 0, 1, (n + 255) / 256, h->queue.p, h->stream)) ||
             (e = cudaEventRecord(ev[2], h->stream)) ||
@@ -833,8 +905,9 @@ int vm_evaluate_loss(vm_optimizer *h, float *loss)
     int rc;
     if ((rc = ensure_grid(h))) return rc;
     cudaError_t e;
-    int lossTiles = (h->liveTargets + h->lossTile - 1) / h->lossTile;
-    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 1, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+    int lossTiles = loss_tiles(h);
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 1, h->lossGrid, h->lossVariant, h->nWindows > 0,
+                            h->queue.p, h->stream)) ||
         (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream)))
         return cuda_fail(e, "evaluate loss");
     VmState st;
@@ -944,8 +1017,9 @@ int vm_probe(vm_optimizer *h, int mode, int *i0, int *j, float *loss, float *gra
     h->fit.dbgLoss = h->dbgLoss.p;
     if ((rc = upload_tables(h))) return rc;
     cudaError_t e;
-    int lossTiles = (live + h->lossTile - 1) / h->lossTile;
-    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, mode, h->lossGrid, h->lossVariant, h->queue.p, h->stream)) ||
+    int lossTiles = loss_tiles(h);
+    if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, mode, h->lossGrid, h->lossVariant, h->nWindows > 0,
+                            h->queue.p, h->stream)) ||
         (e = vm_launch_finalize(h->dFit.p, 1, h->queue.p, h->stream))) {
         h->fit = saved;
         upload_tables(h);

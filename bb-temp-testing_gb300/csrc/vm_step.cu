@@ -242,6 +242,26 @@ __global__ void __launch_bounds__(256) k_block5_max(const int *__restrict__ tsta
     if ((threadIdx.x & 31) == 0 && sum > 0) atomicMax(out, sum);
 }
 
+// The loss windows of a fit's cell-sorted targets: the number of windows of
+// each cell's run (at most 32 targets each), then each window's start.
+__global__ void k_win_count(const int *__restrict__ tstart, int cells, int sub, int *counts)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    int n = tstart[(size_t)(c + 1) << (2 * sub)] - tstart[(size_t)c << (2 * sub)];
+    counts[c] = (n + 31) >> 5;
+}
+
+__global__ void k_win_fill(const int *__restrict__ tstart, int cells, int sub, const int *__restrict__ wstart,
+                           int *twin)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cells) return;
+    int s = tstart[(size_t)c << (2 * sub)], n = tstart[(size_t)(c + 1) << (2 * sub)] - s, w = wstart[c];
+    for (int k = 0; 32 * k < n; ++k) twin[w + k] = s + 32 * k;
+    if (c == cells - 1) twin[wstart[cells]] = tstart[(size_t)cells << (2 * sub)];
+}
+
 // Sparse target update (reference scatterTargetsKernel, voro_optimizer.cu:303-307)
 __global__ void k_scatter_targets(float2 *targets, const int *slots, const float2 *values, int n)
 {
@@ -362,6 +382,19 @@ int vm_fast_shift(int block5Max)
     int bits = 0; // ceil(log2(max(block5Max, 1)))
     while (bits < 31 && (1LL << bits) < (long long)block5Max) ++bits;
     return 38 - bits;
+}
+
+cudaError_t vm_launch_target_windows(const int *tstart, int cells, int sub, const VmPointSet *winSet,
+                                     const int *winPre, int tiles, int *counts, const int *start, int *twin,
+                                     cudaStream_t s)
+{
+    if (cells <= 0) return cudaSuccess;
+    int b = (cells + 255) / 256;
+    k_win_count<<<b, 256, 0, s>>>(tstart, cells, sub, counts);
+    cudaError_t e = vm_launch_scan(winSet, winPre, 1, tiles, s);
+    if (e) return e;
+    k_win_fill<<<b, 256, 0, s>>>(tstart, cells, sub, start, twin);
+    return cudaGetLastError();
 }
 
 cudaError_t vm_launch_scatter_targets(float2 *targets, const int *slots, const float2 *values, int n, cudaStream_t s)

@@ -71,6 +71,11 @@ struct VmFit {
     // optional per-target diagnostics (nullptr unless requested)
     int *dbgI0, *dbgJ;
     float *dbgLoss;
+    // The loss pass's windows (a warp's iteration): nullptr for runs of 32 in
+    // target order; else nWindows cell-aligned runs of at most 32 targets,
+    // twin[w] the start of window w and twin[nWindows] = nTargets.
+    const int *twin;
+    int nWindows;
 };
 
 // A set of points to bin into a fit's hash grid (sites or targets).
