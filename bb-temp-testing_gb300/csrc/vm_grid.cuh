@@ -132,10 +132,11 @@ __device__ __forceinline__ void grid_tile_apply(const VmPointSet &S, int tile)
 // Pass 1 stores each scan tile's sum in the set's tileState word and counts
 // the tile as done; the block that counts a set's last tile (every other
 // tile's sum is then written) turns the set's sums into exclusive prefixes and
-// writes start[cells]. Pass 2 scans each tile from its prefix. Nothing waits,
-// and each tile of pass 2 reads one prefix word instead of every earlier
-// tile's sum. tileState[tiles] (low half) is the set's done counter, zero
-// between scans.
+// writes start[cells]. Pass 2 scans each tile from its prefix and zeroes the
+// prefix word. Nothing waits, and each tile of pass 2 reads one prefix word
+// instead of every earlier tile's sum. tileState[tiles] (low half) is the
+// set's done counter. Every word is zero between scans, so a buffer can serve
+// a later scan of fewer tiles (its done counter then sits on an old tile word).
 __device__ __forceinline__ int grid_tiles(const VmPointSet &S) { return (grid_keys(S) + kScanTile - 1) / kScanTile; }
 
 // The eight counts of this thread in the tile; `zero`: clear them for the next build.
@@ -220,6 +221,9 @@ __device__ __forceinline__ void grid_tile_scan(const VmPointSet &S, int tile)
     grid_load8(S, base, cells, v, true);
     int total;
     int at = offset + block_scan8(v, ws, total);
+    // read by this tile only, by every thread before the scan's barriers:
+    // zero for the next scan
+    if (threadIdx.x == 0) S.tileState[tile] = 0;
     if (base + 8 <= cells) {
         int4 *o = reinterpret_cast<int4 *>(S.start + base);
         o[0] = make_int4(at + v[0], at + v[1], at + v[2], at + v[3]);

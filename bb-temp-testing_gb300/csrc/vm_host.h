@@ -58,7 +58,7 @@ template <class T> struct DevBuf {
 };
 
 // The tile words of a scan over `tiles` tiles (vm_launch_scan): allocated and
-// zeroed when too small, kept otherwise (every scan leaves the done counter zero).
+// zeroed when too small, kept otherwise (every scan leaves all of them zero).
 inline int zeroed_tile_state(DevBuf<unsigned long long> &b, int tiles, cudaStream_t s)
 {
     size_t need = (size_t)tiles + 1;

@@ -9,8 +9,9 @@ cudaError_t vm_launch_bin(const VmPointSet *sets, const int *prefix, int nSets, 
                           cudaStream_t s);
 // Exclusive scan of each set's cell counts into start[] (counts zeroed again),
 // two launches. Each set's tileState holds one word per scan tile and a done
-// counter after them, zero before the first scan (every scan leaves it zero);
-// launches sharing a set's tileState are stream-ordered.
+// counter after them, all zero before the first scan (every scan leaves them
+// zero, so the buffer also serves later scans of fewer tiles); launches
+// sharing a set's tileState are stream-ordered.
 cudaError_t vm_launch_scan(const VmPointSet *sets, const int *tilePrefix, int nSets, int totalTiles, cudaStream_t s);
 cudaError_t vm_launch_scatter(const VmPointSet *sets, const int *prefix, int nSets, int totalBlocks,
                               const VmFit *publish, cudaStream_t s);

@@ -245,3 +245,32 @@ def test_extract_precision_lattice_full_size(vm, orc, capsys):
               f"zero-length edges, {len(rest)} degenerate ({min(len(rest), 40)} checked exact); "
               f"unsafe {mesh.unsafeCells}, watertight {mesh.watertight}")
     assert len(rest) <= n // 100
+
+
+def test_extract_after_slot_grid_shrinks(vm):
+    """Extract on an optimiser whose slot grid shrank (6,000 slots, then
+    1,000: a later cell-packing scan of fewer tiles on the same buffers)
+    gives what a fresh optimiser gives."""
+    from voromesh_gb300 import OptimizerParams, VoroOptimizer, synth
+
+    masks, tiles, voxel = disc_masks()
+    big, small = synth.uniform(43, 1, 6000), synth.uniform(43, 2, 1000)
+
+    def fresh():
+        o = VoroOptimizer(2.0, 2.0, 0.05, OptimizerParams(lossK=12))
+        o.SetTargets(small[:8])
+        o.SetOccupancy(masks, tiles, tiles, voxel)
+        return o
+
+    reused = fresh()
+    reused.SetGenerators(big, len(big), 1, 2.0)
+    reused.Extract()
+    reused.SetGenerators(small, len(small), 1, 2.0)
+    a = reused.Extract()
+    other = fresh()
+    other.SetGenerators(small, len(small), 1, 2.0)
+    b = other.Extract()
+    assert np.array_equal(a.cellStart, b.cellStart)
+    assert np.array_equal(a.cellLabels, b.cellLabels)
+    assert np.array_equal(a.cellVerts.view(np.uint32), b.cellVerts.view(np.uint32))
+    assert np.array_equal(a.edges, b.edges) and a.watertight == b.watertight

@@ -275,3 +275,35 @@ def test_fast_path_gradient_past_int64(vm, orc):
     assert np.array_equal(opt.Generators(), rg)
     assert np.array_equal(om, rm) and np.array_equal(ov, rv)
     assert opt.info().exactTargets == 0
+
+
+def test_loss_windows_follow_the_live_target_count(vm, orc):
+    """The loss pass's windows follow every target change: 540,000 live
+    targets walk windows of 32 in target order, 513,000 (under 2^19)
+    cell-aligned windows, then 540,000 again; every phase steps exactly as
+    the oracle."""
+    from voromesh_gb300 import synth
+
+    from voromesh_gb300 import OptimizerParams, VoroOptimizer
+
+    gen = synth.uniform(8, 1, 2048)
+    tgt = synth.circle(8, 2, 540000, 0.6, 2e-3)
+    opt = VoroOptimizer(2.0, 2.0, 0.05, OptimizerParams(iterations=60, sampleFraction=1.0, lossK=12))
+    opt.SetTargets(tgt)
+    opt.SetGenerators(gen, len(gen), 1, 2.0)
+    ref = orc.Fit(2.0, 2.0, 0.05, 12, 0.09, 1.0, 60, nthreads=8)
+    ref.set_targets(tgt)
+    ref.set_generators(gen, len(gen), 1, 2.0)
+    cur = tgt.copy()
+    drop = np.arange(0, len(tgt), 20)  # 27,000 targets
+    for phase in range(3):
+        if phase:
+            cur[drop] = -1.0 if phase == 1 else tgt[drop]
+            opt.UpdateTargets(drop, cur)
+            ref.set_targets(cur)
+        opt.Step(2)
+        lref = ref.step(2)
+        g, m, v = ref.generators()
+        assert np.array_equal(opt.Generators(), g), phase
+        assert np.float32(opt.LastBatchLoss()) == np.float32(lref)
+        assert opt.info().liveTargets == (513000 if phase == 1 else 540000)
