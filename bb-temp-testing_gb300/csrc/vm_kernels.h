@@ -39,11 +39,16 @@ cudaError_t vm_launch_target_windows(const int *tstart, int cells, int sub, cons
 int vm_loss_variants();
 int vm_loss_variant_threads(int variant);
 // A fit of at most 4,096 slots and 8,192 grid cells can end its step in one
-// block: Adam, binning, scan and scatter (in place of vm_launch_adam_bin,
-// vm_launch_scan and vm_launch_scatter with publish), for the one fit of the
-// table `fit`.
+// block after vm_launch_loss_fast: the deferred targets and Adam schedule,
+// Adam, binning, scan and scatter (in place of the exact pass of
+// vm_launch_loss, vm_launch_adam_bin, vm_launch_scan and vm_launch_scatter
+// with publish), for the one fit of the table `fit`.
 bool vm_small_grid_fits(int slots, int cells);
 cudaError_t vm_launch_small_grid(const VmFit *fit, void *queue, cudaStream_t s);
+// The fast path of vm_launch_loss alone (a step pass; its deferred targets
+// and schedule are left to vm_launch_small_grid).
+cudaError_t vm_launch_loss_fast(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int gridBlocks,
+                                int variant, int windowed, void *queue, cudaStream_t s);
 cudaError_t vm_launch_finalize(const VmFit *fits, int nFits, void *queue, cudaStream_t s);
 cudaError_t vm_launch_adam_bin(const VmFit *fits, const int *prefix, int nFits, int totalBlocks, void *queue,
                                cudaStream_t s);

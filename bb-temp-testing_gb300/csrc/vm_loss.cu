@@ -7,6 +7,7 @@
 //                 targets go to a queue
 //   k_loss_exact  the queued targets: exact ring search, one per thread
 #include "vm_device.cuh"
+#include "vm_adam.cuh"
 #include "vm_knn.cuh"
 #include "vm_kernels.h"
 
@@ -783,10 +784,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // into its exact split words. In a step pass it also writes each fit's Adam
 // schedule for the step, and recomputes the whole gradient of every fit whose
 // fast-path bound failed (its deferred targets are then part of that).
-__global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fits, int nFits, int mode,
-                                                    SlowQueue *queue)
+// The body of k_loss_exact for thread `tid` of `stride` threads.
+__device__ __forceinline__ void exact_pass(const VmFit *__restrict__ fits, int nFits, int mode, SlowQueue *queue,
+                                           int tid, int stride)
 {
-    int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     if (mode == 0)
         for (int f = tid; f < nFits; f += stride)
             if (fits[f].active) adam_schedule(fits[f]); // for the Adam kernel that follows
@@ -832,6 +833,141 @@ __global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fi
         }
     }
 }
+
+__global__ void __launch_bounds__(128) k_loss_exact(const VmFit *__restrict__ fits, int nFits, int mode,
+                                                    SlowQueue *queue)
+{
+    exact_pass(fits, nFits, mode, queue, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// The exact pass of one fit by one block (out of line: it is the rare path,
+// and its registers stay out of the caller's).
+static __device__ __noinline__ void exact_pass_block(const VmFit *__restrict__ fits, SlowQueue *queue)
+{
+    exact_pass(fits, 1, 0, queue, threadIdx.x, blockDim.x);
+}
+
+// A fit this small finishes its step in one block (k_small_grid).
+constexpr int kSmallThreads = 1024;
+constexpr int kSmallSlots = 4 * kSmallThreads;
+constexpr int kSmallCells = 8 * kSmallThreads;
+
+// The rest of a small fit's step in one block (k_loss_exact, k_adam_bin,
+// k_scan_tiles, k_scan_apply and k_scatter for one fit of at most kSmallSlots
+// slots and kSmallCells grid cells): the deferred targets and the Adam
+// schedule, then Adam with the binning into shared-memory counts, their
+// exclusive scan in place, the cell starts, the scatter and the publish. Ranks within a cell come from the shared atomics, in another order
+// than the four-kernel path; nothing in the step depends on that order.
+__global__ void __launch_bounds__(kSmallThreads) k_small_grid(const VmFit *__restrict__ fits, SlowQueue *queue)
+{
+    __shared__ int sStart[kSmallCells + 1];
+    __shared__ int sWarp[kSmallThreads / 32];
+    __shared__ int sTotal;
+    constexpr int kPer = kSmallSlots / kSmallThreads;
+    const VmFit &F = fits[0];
+    int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int n = F.nSlots, cells = F.gridW * F.gridH;
+    // the deferred targets and the schedule; their writes are visible to the
+    // whole block after the barrier
+    exact_pass_block(fits, queue);
+    for (int c = tid; c <= cells; c += kSmallThreads) sStart[c] = 0;
+    __syncthreads();
+    if (tid == 0) {
+        queue->count = 0;
+        queue->nFlagged = 0;
+    }
+    // Adam and the binning
+    int key[kPer], rank[kPer];
+    float2 pos[kPer];
+    if (F.active) {
+        AdamStep a = adam_step(F);
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            int i = tid + k * kSmallThreads;
+            key[k] = -1;
+            if (i < n) {
+                pos[k] = adam_slot(F, a, i);
+                if (pos[k].x >= 0.0f) {
+                    key[k] = cell_coord(pos[k].y, F.inv, F.gridH) * F.gridW + cell_coord(pos[k].x, F.inv, F.gridW);
+                    rank[k] = atomicAdd(&sStart[key[k]], 1);
+                }
+            }
+        }
+    } else {
+        // a fit left out of the step keeps its positions: re-bin them
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            int i = tid + k * kSmallThreads;
+            key[k] = -1;
+            if (i < n) {
+                pos[k] = F.gen[i];
+                if (pos[k].x >= 0.0f) {
+                    key[k] = cell_coord(pos[k].y, F.inv, F.gridH) * F.gridW + cell_coord(pos[k].x, F.inv, F.gridW);
+                    rank[k] = atomicAdd(&sStart[key[k]], 1);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // exclusive scan of the counts in place (8 cells a thread), total at [cells]
+    int v[8], base = tid * 8, run = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int x = base + k < cells ? sStart[base + k] : 0;
+        v[k] = run;
+        run += x;
+    }
+    int incl = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int t = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += t;
+    }
+    if (lane == 31) sWarp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = sWarp[lane], wi = w;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int t = __shfl_up_sync(kFull, wi, off);
+            if (lane >= off) wi += t;
+        }
+        sWarp[lane] = wi - w;
+        if (lane == 31) sTotal = wi;
+    }
+    __syncthreads();
+    int excl = incl - run + sWarp[warp];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (base + k < cells) sStart[base + k] = excl + v[k];
+    if (tid == 0) sStart[cells] = sTotal;
+    __syncthreads();
+    for (int c = tid; c <= cells; c += kSmallThreads) F.start[c] = sStart[c];
+    // the slots' cell keys (exported with the grid) and the cell-sorted copy
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+        if (tid + k * kSmallThreads < n) F.key[tid + k * kSmallThreads] = key[k];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+        if (key[k] >= 0) {
+            int at = sStart[key[k]] + rank[k];
+            F.sortedIdx[at] = tid + k * kSmallThreads;
+            F.sortedPos[at] = pos[k];
+        }
+    if (tid == 0 && F.active) {
+        // end of a step: publish the loss pass and advance the step counter
+        VmState *st = F.state;
+        st->loss = fxl_to_float(st->accLo, st->accHi, F.lossExp);
+        st->count = st->accCount;
+        st->iter += 1;
+        st->accLo = 0;
+        st->accHi = 0;
+        st->accCount = 0;
+        st->needExact = 0;
+        st->dUsed = 0;
+    }
+}
+
 
 } // namespace vmk
 
@@ -891,6 +1027,27 @@ cudaError_t vm_launch_loss(const VmFit *fits, const int *tilePrefix, int nFits, 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     k_loss_exact<<<sms * 2, 128, 0, s>>>(fits, nFits, mode, q);
     return cudaGetLastError();
+}
+
+bool vm_small_grid_fits(int slots, int cells) { return slots <= kSmallSlots && cells <= kSmallCells; }
+
+cudaError_t vm_launch_small_grid(const VmFit *fit, void *queue, cudaStream_t s)
+{
+    k_small_grid<<<1, kSmallThreads, 0, s>>>(fit, static_cast<SlowQueue *>(queue));
+    return cudaGetLastError();
+}
+
+cudaError_t vm_launch_loss_fast(const VmFit *fits, const int *tilePrefix, int nFits, int totalTiles, int gridBlocks,
+                                int variant, int windowed, void *queue, cudaStream_t s)
+{
+    if (totalTiles <= 0) return cudaSuccess;
+    SlowQueue *q = static_cast<SlowQueue *>(queue);
+    int mode = 0;
+    int g = gridBlocks < totalTiles ? gridBlocks : totalTiles;
+    if (g < 1) g = 1;
+    void *args[] = {(void *)&fits, (void *)&tilePrefix, (void *)&nFits, (void *)&mode, (void *)&q};
+    return cudaLaunchKernel(variant_fn(variant, windowed != 0), dim3(g), dim3(vm_loss_variant_threads(variant)), args, 0,
+                            s);
 }
 
 int vm_loss_occupancy_blocks(int variant)

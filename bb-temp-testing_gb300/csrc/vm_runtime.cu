@@ -334,14 +334,17 @@ int enqueue_step(vm_optimizer *h)
     int n = h->numSlots();
     cudaError_t e;
     int lossTiles = loss_tiles(h);
+    if (vm_small_grid_fits(n, h->cells)) {
+        // the loss fast path, then the rest of the step in one block
+        if ((e = vm_launch_loss_fast(h->dFit.p, h->dPre.p + 4, 1, lossTiles, h->lossGrid, h->lossVariant,
+                                     h->nWindows > 0, h->queue.p, h->stream)) ||
+            (e = vm_launch_small_grid(h->dFit.p, h->queue.p, h->stream)))
+            return cuda_fail(e, "small step");
+        return VM_OK;
+    }
     if ((e = vm_launch_loss(h->dFit.p, h->dPre.p + 4, 1, lossTiles, 0, h->lossGrid, h->lossVariant, h->nWindows > 0,
                             h->queue.p, h->stream)))
         return cuda_fail(e, "loss");
-    if (vm_small_grid_fits(n, h->cells)) {
-        // Adam, the grid rebuild and the publish in one block
-        if ((e = vm_launch_small_grid(h->dFit.p, h->queue.p, h->stream))) return cuda_fail(e, "small grid");
-        return VM_OK;
-    }
     if ((e = vm_launch_adam_bin(h->dFit.p, h->dPre.p + 0, 1, (n + 255) / 256, h->queue.p, h->stream)))
         return cuda_fail(e, "adam");
     if ((e = vm_launch_scan(h->dSites.p, h->dPre.p + 2, 1, h->tiles, h->stream))) return cuda_fail(e, "scan");

@@ -20,6 +20,7 @@
 // order within a cell's run (every argmin breaks ties by index, every sum is
 // exact), so k_canonical runs only before the grid is exported.
 #include "vm_device.cuh"
+#include "vm_adam.cuh"
 #include "vm_grid.cuh"
 #include "vm_knn.cuh"
 #include "vm_kernels.h"
@@ -34,10 +35,6 @@ constexpr int kSiteBlock = 256;
 constexpr int kSiteThreads = 64;
 constexpr int kSitesPerThread = kSiteBlock / kSiteThreads;
 
-// A fit this small finishes its step in one block (k_small_grid).
-constexpr int kSmallThreads = 1024;
-constexpr int kSmallSlots = 4 * kSmallThreads;
-constexpr int kSmallCells = 8 * kSmallThreads;
 
 // ---------------------------------------------------------------------------
 // hash grid build over a table of point sets (bodies in vm_grid.cuh)
@@ -144,95 +141,6 @@ __global__ void k_finalize(const VmFit *__restrict__ fits, int nFits, SlowQueue 
 // slot's loads are issued together, and 32 registers keep 8 blocks resident
 // per SM (measured faster than 45 registers at 5 blocks).
 // ---------------------------------------------------------------------------
-// This step's Adam values of a fit, read once per thread: the lr and bias
-// corrections (adam_schedule, run by the loss pass), the gradient's 1 / count,
-// and which gradient words hold the sums.
-struct AdamStep {
-    float lr, bc1, bc2, scale;
-    bool split, useL;
-};
-
-__device__ __forceinline__ AdamStep adam_step(const VmFit &F)
-{
-    const VmState *st = F.state;
-    AdamStep a;
-    a.lr = st->schedLr;
-    a.bc1 = st->schedBc1;
-    a.bc2 = st->schedBc2;
-    int count = st->accCount;
-    a.scale = 1.0f / (float)(count > 1 ? count : 1);
-    a.split = (st->dUsed | st->needExact) != 0;
-    a.useL = !st->needExact;
-    return a;
-}
-
-// Adam and the clamp for slot i (reference adamKernel, voro_optimizer.cu:271-301):
-// reads and clears the slot's gradient words, updates gen, m and v; returns
-// the slot's new position (x < 0: an empty slot).
-__device__ __forceinline__ float2 adam_slot(const VmFit &F, const AdamStep &a, int i)
-{
-    // this slot's gradient: section L of gradX (one 64-bit sum per component)
-    // or, when the pass used the exact split words (deferred targets, or a
-    // fit whose fast-path bound failed), the exact sum of all three sections;
-    // the words are cleared for the next step
-    longlong2 *gw = reinterpret_cast<longlong2 *>(F.gradX) + i;
-    // the slot's words are loaded together (m and v also for an empty slot,
-    // which leaves them unused)
-    longlong2 gl = gw[0];
-    float2 p = F.gen[i], m = F.m[i], v = F.v[i];
-    if (gl.x | gl.y) gw[0] = make_longlong2(0, 0);
-    float lr = a.lr, bc1 = a.bc1, bc2 = a.bc2, scale = a.scale;
-    float grx, gry;
-    if (!a.split) {
-        // a zero sum is +0 either way; it skips the 64-bit conversion
-        grx = gl.x ? scale * fx_to_float(gl.x, F.gradExp) : 0.0f;
-        gry = gl.y ? scale * fx_to_float(gl.y, F.gradExp) : 0.0f;
-    } else {
-        size_t sec = (size_t)F.nSlots;
-        longlong2 gdl = gw[sec], gdh = gw[2 * sec];
-        gw[sec] = make_longlong2(0, 0);
-        gw[2 * sec] = make_longlong2(0, 0);
-        grx = scale * fx_site_to_float(gl.x, a.useL, (unsigned long long)gdl.x, gdh.x, F.gradExp);
-        gry = scale * fx_site_to_float(gl.y, a.useL, (unsigned long long)gdl.y, gdh.y, F.gradExp);
-    }
-    bool inRegion = true;
-    if (F.cx0 != 0 || F.cy0 != 0 || F.cx1 != F.slotsW || F.cy1 != F.slotsH) {
-        int sx = i % F.slotsW, sy = i / F.slotsW;
-        inRegion = sx >= F.cx0 && sx < F.cx1 && sy >= F.cy0 && sy < F.cy1;
-    }
-    if (p.x >= 0.0f && inRegion) {
-        float b1 = F.beta1, b2 = F.beta2, eps = F.eps;
-        // A slot with a zero gradient and zero moments: the update keeps the
-        // moments at +0 and subtracts +0 from p (+0 / bc1 = +0, sqrtf(+0) + eps
-        // = eps, lr * +0 / eps = +0, p - +0 = p for every p), so only the clamp
-        // acts. Exact for lr, bc1, bc2, eps > 0 and finite beta1, beta2
-        // (checked); the slots far from every target take this path.
-        bool idle = (__float_as_uint(grx) | __float_as_uint(gry) | __float_as_uint(m.x) | __float_as_uint(m.y) |
-                     __float_as_uint(v.x) | __float_as_uint(v.y)) == 0u &&
-                    lr > 0.0f && lr < FLT_MAX && bc1 > 0.0f && bc2 > 0.0f && eps > 0.0f && fabsf(b1) < FLT_MAX &&
-                    fabsf(b2) < FLT_MAX;
-        if (idle) {
-            float2 q = make_float2(fminf(fmaxf(p.x, 0.0f), F.width), fminf(fmaxf(p.y, 0.0f), F.height));
-            if (__float_as_uint(q.x) != __float_as_uint(p.x) || __float_as_uint(q.y) != __float_as_uint(p.y))
-                F.gen[i] = q;
-            p = q;
-        } else {
-            float mx = b1 * m.x + (1.0f - b1) * grx;
-            float my = b1 * m.y + (1.0f - b1) * gry;
-            float vx = b2 * v.x + (1.0f - b2) * (grx * grx);
-            float vy = b2 * v.y + (1.0f - b2) * (gry * gry);
-            F.m[i] = make_float2(mx, my);
-            F.v[i] = make_float2(vx, vy);
-            p.x -= lr * (mx / bc1) / (sqrtf(vx / bc2) + eps);
-            p.y -= lr * (my / bc1) / (sqrtf(vy / bc2) + eps);
-            p.x = fminf(fmaxf(p.x, 0.0f), F.width);
-            p.y = fminf(fmaxf(p.y, 0.0f), F.height);
-            F.gen[i] = p;
-        }
-    }
-    return p;
-}
-
 __global__ void __launch_bounds__(256, 8) k_adam_bin(const VmFit *__restrict__ fits, const int *__restrict__ prefix,
                                                   int nFits, SlowQueue *queue)
 {
@@ -253,119 +161,6 @@ __global__ void __launch_bounds__(256, 8) k_adam_bin(const VmFit *__restrict__ f
     int c = cell_coord(p.y, F.inv, F.gridH) * F.gridW + cell_coord(p.x, F.inv, F.gridW);
     F.key[i] = c;
     F.rank[i] = atomicAdd(&F.counts[c], 1);
-}
-
-// The rest of a small fit's step in one block (k_adam_bin, k_scan_tiles,
-// k_scan_apply and k_scatter for one fit of at most kSmallSlots slots and
-// kSmallCells grid cells): Adam with the binning into shared-memory counts,
-// their exclusive scan in place, the cell starts, the scatter and the
-// publish. Ranks within a cell come from the shared atomics, in another order
-// than the four-kernel path; nothing in the step depends on that order.
-__global__ void __launch_bounds__(kSmallThreads) k_small_grid(const VmFit *__restrict__ fits, SlowQueue *queue)
-{
-    __shared__ int sStart[kSmallCells + 1];
-    __shared__ int sWarp[kSmallThreads / 32];
-    __shared__ int sTotal;
-    constexpr int kPer = kSmallSlots / kSmallThreads;
-    const VmFit &F = fits[0];
-    int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    int n = F.nSlots, cells = F.gridW * F.gridH;
-    if (tid == 0) {
-        queue->count = 0;
-        queue->nFlagged = 0;
-    }
-    for (int c = tid; c <= cells; c += kSmallThreads) sStart[c] = 0;
-    __syncthreads();
-    // Adam and the binning
-    int key[kPer], rank[kPer];
-    float2 pos[kPer];
-    if (F.active) {
-        AdamStep a = adam_step(F);
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-            int i = tid + k * kSmallThreads;
-            key[k] = -1;
-            if (i < n) {
-                pos[k] = adam_slot(F, a, i);
-                if (pos[k].x >= 0.0f) {
-                    key[k] = cell_coord(pos[k].y, F.inv, F.gridH) * F.gridW + cell_coord(pos[k].x, F.inv, F.gridW);
-                    rank[k] = atomicAdd(&sStart[key[k]], 1);
-                }
-            }
-        }
-    } else {
-        // a fit left out of the step keeps its positions: re-bin them
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-            int i = tid + k * kSmallThreads;
-            key[k] = -1;
-            if (i < n) {
-                pos[k] = F.gen[i];
-                if (pos[k].x >= 0.0f) {
-                    key[k] = cell_coord(pos[k].y, F.inv, F.gridH) * F.gridW + cell_coord(pos[k].x, F.inv, F.gridW);
-                    rank[k] = atomicAdd(&sStart[key[k]], 1);
-                }
-            }
-        }
-    }
-    __syncthreads();
-    // exclusive scan of the counts in place (8 cells a thread), total at [cells]
-    int v[8], base = tid * 8, run = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        int x = base + k < cells ? sStart[base + k] : 0;
-        v[k] = run;
-        run += x;
-    }
-    int incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        int t = __shfl_up_sync(kFull, incl, off);
-        if (lane >= off) incl += t;
-    }
-    if (lane == 31) sWarp[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        int w = sWarp[lane], wi = w;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            int t = __shfl_up_sync(kFull, wi, off);
-            if (lane >= off) wi += t;
-        }
-        sWarp[lane] = wi - w;
-        if (lane == 31) sTotal = wi;
-    }
-    __syncthreads();
-    int excl = incl - run + sWarp[warp];
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (base + k < cells) sStart[base + k] = excl + v[k];
-    if (tid == 0) sStart[cells] = sTotal;
-    __syncthreads();
-    for (int c = tid; c <= cells; c += kSmallThreads) F.start[c] = sStart[c];
-    // the slots' cell keys (exported with the grid) and the cell-sorted copy
-#pragma unroll
-    for (int k = 0; k < kPer; ++k)
-        if (tid + k * kSmallThreads < n) F.key[tid + k * kSmallThreads] = key[k];
-#pragma unroll
-    for (int k = 0; k < kPer; ++k)
-        if (key[k] >= 0) {
-            int at = sStart[key[k]] + rank[k];
-            F.sortedIdx[at] = tid + k * kSmallThreads;
-            F.sortedPos[at] = pos[k];
-        }
-    if (tid == 0 && F.active) {
-        // end of a step: publish the loss pass and advance the step counter
-        VmState *st = F.state;
-        st->loss = fxl_to_float(st->accLo, st->accHi, F.lossExp);
-        st->count = st->accCount;
-        st->iter += 1;
-        st->accLo = 0;
-        st->accHi = 0;
-        st->accCount = 0;
-        st->needExact = 0;
-        st->dUsed = 0;
-    }
 }
 
 // The largest number of targets in any 5x5 block of hash cells (the bound
@@ -471,14 +266,6 @@ cudaError_t vm_launch_scatter(const VmPointSet *sets, const int *prefix, int nSe
 {
     if (totalBlocks <= 0) return cudaSuccess;
     k_scatter<<<totalBlocks, kSiteThreads, 0, s>>>(sets, prefix, nSets, publish);
-    return cudaGetLastError();
-}
-
-bool vm_small_grid_fits(int slots, int cells) { return slots <= kSmallSlots && cells <= kSmallCells; }
-
-cudaError_t vm_launch_small_grid(const VmFit *fit, void *queue, cudaStream_t s)
-{
-    k_small_grid<<<1, kSmallThreads, 0, s>>>(fit, static_cast<SlowQueue *>(queue));
     return cudaGetLastError();
 }
 
