@@ -125,9 +125,43 @@ struct vmb_batch {
     bool dirty = true;
     std::vector<VmState> hostStates;
     DevBuf<int> block5Buf; // a fit's largest 5x5-block target count, read back at vmb_add_fit
+    // pinned staging of host-to-device copies (a copy from pageable memory
+    // would first wait for the stream); reused from its start after a sync
+    char *hstage = nullptr;
+    size_t hstageCap = 0, hstageUsed = 0;
 };
 
 namespace {
+
+// Copies `bytes` from `src` into the pinned staging buffer and enqueues their
+// copy to `dst` on the batch stream. The staged bytes stay untouched until
+// the next stream sync (staging_done), so nothing waits here.
+cudaError_t stage_copy(vmb_batch *b, void *dst, const void *src, size_t bytes)
+{
+    if (!bytes) return cudaSuccess;
+    size_t room = (bytes + 255) & ~(size_t)255;
+    if (b->hstageUsed + room > b->hstageCap) {
+        // earlier staged copies may still be reading the buffer
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e) return e;
+        b->hstageUsed = 0;
+        if (room > b->hstageCap) {
+            if (b->hstage) cudaFreeHost(b->hstage);
+            b->hstage = nullptr;
+            b->hstageCap = 0;
+            size_t cap = std::max(room, (size_t)1 << 22);
+            if ((e = cudaMallocHost((void **)&b->hstage, cap))) return e;
+            b->hstageCap = cap;
+        }
+    }
+    char *p = b->hstage + b->hstageUsed;
+    std::memcpy(p, src, bytes);
+    b->hstageUsed += room;
+    return cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, b->stream);
+}
+
+// After a sync of the batch stream every staged copy has been read.
+void staging_done(vmb_batch *b) { b->hstageUsed = 0; }
 
 int single_set_build(vmb_batch *b, const VmPointSet &S, int emptyIsNegative, int canonical)
 {
@@ -138,12 +172,10 @@ int single_set_build(vmb_batch *b, const VmPointSet &S, int emptyIsNegative, int
     int tiles = (int)((keys + kScanTile - 1) / kScanTile);
     int pre[4] = {0, blocks, 0, tiles};
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(b->dOneSet.p, &T, sizeof(T), cudaMemcpyHostToDevice, b->stream)) ||
-        (e = cudaMemcpyAsync(b->dOnePre.p, pre, sizeof(pre), cudaMemcpyHostToDevice, b->stream)) ||
+    if ((e = stage_copy(b, b->dOneSet.p, &T, sizeof(T))) || (e = stage_copy(b, b->dOnePre.p, pre, sizeof(pre))) ||
         (e = vm_launch_bin(b->dOneSet.p, b->dOnePre.p, 1, blocks, emptyIsNegative, b->stream)) ||
         (e = vm_launch_scan(b->dOneSet.p, b->dOnePre.p + 2, 1, tiles, b->stream)) ||
-        (e = vm_launch_scatter(b->dOneSet.p, b->dOnePre.p, 1, blocks, nullptr, b->stream)) ||
-        (e = cudaStreamSynchronize(b->stream))) // the tables above live on the host stack
+        (e = vm_launch_scatter(b->dOneSet.p, b->dOnePre.p, 1, blocks, nullptr, b->stream)))
         return cuda_fail(e, "batch grid build");
     return VM_OK;
 }
@@ -186,6 +218,7 @@ int rebuild_tables(vmb_batch *b)
         (e = vm_queue_init(b->queue.p, b->qitems.p, (int)b->qitems.n, b->stream)) ||
         (e = cudaStreamSynchronize(b->stream)))
         return cuda_fail(e, "batch tables");
+    staging_done(b);
     b->dirty = false;
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
@@ -294,6 +327,7 @@ int vmb_destroy(vmb_batch *b)
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->hstage) cudaFreeHost(b->hstage);
     delete b;
     return VM_OK;
 }
@@ -423,7 +457,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
                         D.tpos, D.tslot, 0, 1};
     f.tset.tileState = D.tileState;
     cudaError_t e;
-    if ((n && ((e = cudaMemcpyAsync(D.gen, in->generators, sizeof(float2) * n, cudaMemcpyHostToDevice, b->stream)) ||
+    if ((n && ((e = stage_copy(b, D.gen, in->generators, sizeof(float2) * n)) ||
                (e = cudaMemsetAsync(D.m, 0, 8 * (size_t)n, b->stream)) ||
                (e = cudaMemsetAsync(D.v, 0, 8 * (size_t)n, b->stream)) ||
                (e = cudaMemsetAsync(D.gradX, 0, 8 * kGradWords * (size_t)n, b->stream)))) ||
@@ -431,8 +465,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
         (e = cudaMemsetAsync(D.tileState, 0, 8 * ((size_t)f.tiles + 1), b->stream)) ||
         (e = cudaMemsetAsync(D.state, 0, sizeof(VmState), b->stream)) ||
         (e = cudaMemsetAsync(f.traw, 0xFF, 8 * (size_t)f.cap, b->stream)) ||
-        (in->nTargets && (e = cudaMemcpyAsync(f.traw, in->targets, 8 * (size_t)in->nTargets, cudaMemcpyHostToDevice,
-                                              b->stream)))) {
+        (in->nTargets && (e = stage_copy(b, f.traw, in->targets, 8 * (size_t)in->nTargets)))) {
         release_fit(b, f);
         return cuda_fail(e, "vmb_add_fit upload");
     }
@@ -488,6 +521,7 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
         release_fit(b, f);
         return cuda_fail(e, "vmb_add_fit live targets");
     }
+    staging_done(b);
     releaseTmp();
     f.liveTargets = live;
     D.nTargets = live;
