@@ -307,3 +307,40 @@ def test_loss_windows_follow_the_live_target_count(vm, orc):
         assert np.array_equal(opt.Generators(), g), phase
         assert np.float32(opt.LastBatchLoss()) == np.float32(lref)
         assert opt.info().liveTargets == (513000 if phase == 1 else 540000)
+
+
+@pytest.mark.parametrize("slots_w,slots_h,width,spacing", [
+    (64, 64, 2.0, 2.0 / 128),   # 4,096 slots, 128 x 64 = 8,192 cells: the one-block step
+    (4097, 1, 2.0, 2.0 / 128),  # one slot more: the six-kernel step
+    (64, 64, 2.0, 2.0 / 129),   # 129 x 65 cells: the six-kernel step
+])
+def test_step_at_the_small_fit_limits(vm, orc, slots_w, slots_h, width, spacing):
+    """Fits at and just past the one-block step's limits (4,096 slots, 8,192
+    grid cells) step exactly as the oracle, through a milestone."""
+    from voromesh_gb300 import OptimizerParams, VoroOptimizer, synth
+
+    n = slots_w * slots_h
+    # sites over [0,2] x [0,1], targets on a circle inside it
+    gen = (synth.uniform(31, 1, n, -1.0, 1.0, shift=False) * np.float32([1.0, 0.5]) + np.float32([1.0, 0.5]))
+    gen = gen.astype(np.float32)
+    gen[::9] = -1.0  # empty slots
+    tgt = (synth.circle(31, 2, 6000, 0.4, 1e-3, shift=False) + np.float32([1.0, 0.5])).astype(np.float32)
+    p = OptimizerParams(iterations=40, sampleFraction=0.5, lossK=12, milestones=(6, 30, 35, 38))
+    opt = VoroOptimizer(width, 1.0, spacing, p)
+    opt.SetTargets(tgt)
+    cs = max(2.0 / slots_w, 1.0 / slots_h)  # the slot rectangle covers the domain: every target takes part
+    opt.SetGenerators(gen, slots_w, slots_h, cs)
+    ref = orc.Fit(width, 1.0, spacing, 12, 0.09, 0.5, 40, milestones=(6, 30, 35, 38), nthreads=4)
+    ref.set_targets(tgt)
+    ref.set_generators(gen, slots_w, slots_h, cs)
+    for chunk in (3, 5):
+        opt.Step(chunk)
+        lref = ref.step(chunk)
+        g, m, v = ref.generators()
+        assert np.array_equal(opt.Generators(), g)
+        om, ov = opt.Moments()
+        assert np.array_equal(om, m) and np.array_equal(ov, v)
+        assert np.float32(opt.LastBatchLoss()) == np.float32(lref)
+    start, sidx, spos, gcell = opt.Grid()
+    r = ref.grid()
+    assert np.array_equal(start, r[0]) and np.array_equal(sidx, r[1]) and np.array_equal(gcell, r[3])
