@@ -101,6 +101,9 @@ struct PdJob {
     int x0, y0, x1, y1, trials;
     unsigned roundBase;
 };
+// The jobs' regions packed into out, job k's row-major cells at offsets[k]
+// (jobs and offsets in device memory).
+cudaError_t pd_launch_gather_regions(const PdJob *jobs, const int *offsets, int n, float2 *out, cudaStream_t s);
 // 1 when the region runs as one block (every phase in one pass of it).
 int pd_small_region(int x0, int y0, int x1, int y1);
 // Small regions of distinct samplers (jobs in device memory), one block each.

@@ -129,9 +129,30 @@ __global__ void __launch_bounds__(kSmallBlock) k_resample_many(const PdJob *__re
     resample_block(j.grid, j.p, j.x0, j.y0, j.x1, j.y1, j.trials, j.roundBase);
 }
 
+// The cells of each job's region, packed row by row at out + offsets[job]
+// (one block per job): one copy to the host serves every region.
+__global__ void __launch_bounds__(256) k_gather_regions(const PdJob *__restrict__ jobs, const int *__restrict__ offsets,
+                                                        float2 *__restrict__ out)
+{
+    PdJob j = jobs[blockIdx.x];
+    int w = j.x1 - j.x0, cells = w * (j.y1 - j.y0);
+    float2 *o = out + offsets[blockIdx.x];
+    for (int c = threadIdx.x; c < cells; c += blockDim.x) {
+        int y = j.y0 + c / w, x = j.x0 + c % w;
+        o[c] = j.grid[(size_t)y * j.p.gridW + x];
+    }
+}
+
 } // namespace vmk
 
 using namespace vmk;
+
+cudaError_t pd_launch_gather_regions(const PdJob *jobs, const int *offsets, int n, float2 *out, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    k_gather_regions<<<n, 256, 0, s>>>(jobs, offsets, out);
+    return cudaGetLastError();
+}
 
 cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int trials,
                                unsigned roundBase, cudaStream_t s, bool dependentLaunch)

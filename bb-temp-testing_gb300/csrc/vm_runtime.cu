@@ -1353,6 +1353,14 @@ int vm_update_from_canvas(vm_optimizer *h, cv_canvas *c)
 // ===========================================================================
 } // extern "C"
 
+namespace {
+// Pinned staging of pd_resample_many's job table and packed regions (shared
+// by every sampler of the process; calls take turns).
+std::mutex g_pdStageMu;
+char *g_pdStage = nullptr;
+size_t g_pdStageCap = 0;
+} // namespace
+
 struct pd_sampler {
     float width, height, radius, cellSize;
     int gridW, gridH, trials;
@@ -1469,7 +1477,10 @@ int pd_resample_many(pd_sampler *const *samplers, const int *regions, int n, flo
             total += ms;
             continue;
         }
-        if ((e = cudaStreamSynchronize(s->stream))) return cuda_fail(e, "pd_resample_many sync");
+        // the sampler's own stream must be done with its grid (usually it is idle)
+        e = cudaStreamQuery(s->stream);
+        if (e == cudaErrorNotReady) e = cudaStreamSynchronize(s->stream);
+        if (e) return cuda_fail(e, "pd_resample_many sync");
         PdParams p{s->width, s->height, s->radius, s->cellSize, s->gridW, s->gridH, s->seed};
         jobs.push_back(PdJob{s->grid.p, p, x0, y0, x1, y1, s->trials, s->roundBase});
         jobOf.push_back(i);
@@ -1477,27 +1488,50 @@ int pd_resample_many(pd_sampler *const *samplers, const int *regions, int n, flo
     if (!jobs.empty()) {
         pd_sampler *s0 = samplers[jobOf[0]];
         cudaStream_t st = s0->stream;
-        PdJob *dJobs = nullptr;
-        size_t bytes = sizeof(PdJob) * jobs.size();
-        if ((e = cudaMallocAsync((void **)&dJobs, bytes, st))) return cuda_fail(e, "pd_resample_many jobs");
-        if ((e = cudaMemcpyAsync(dJobs, jobs.data(), bytes, cudaMemcpyHostToDevice, st)) ||
-            (e = cudaEventRecord(s0->ev0, st)) || (e = pd_launch_resample_many(dJobs, (int)jobs.size(), st)) ||
-            (e = cudaEventRecord(s0->ev1, st))) {
-            cudaFreeAsync(dJobs, st);
+        // the regions come back packed: one device-to-host copy for all of them
+        int nj = (int)jobs.size();
+        std::vector<int> offsets(nj + 1, 0);
+        for (int k = 0; k < nj; ++k)
+            offsets[k + 1] = offsets[k] + (jobs[k].x1 - jobs[k].x0) * (jobs[k].y1 - jobs[k].y0);
+        size_t jobBytes = sizeof(PdJob) * nj, offBytes = sizeof(int) * (size_t)(nj + 1);
+        size_t cellBytes = sizeof(float2) * (size_t)offsets[nj];
+        size_t offAt = (jobBytes + 255) & ~(size_t)255, cellAt = offAt + ((offBytes + 255) & ~(size_t)255);
+        std::lock_guard<std::mutex> lk(g_pdStageMu);
+        if (g_pdStageCap < cellAt + cellBytes) {
+            if (g_pdStage) cudaFreeHost(g_pdStage);
+            g_pdStage = nullptr;
+            g_pdStageCap = 0;
+            size_t cap = std::max(cellAt + cellBytes, (size_t)1 << 20);
+            if ((e = cudaMallocHost((void **)&g_pdStage, cap))) return cuda_fail(e, "pd_resample_many staging");
+            g_pdStageCap = cap;
+        }
+        std::memcpy(g_pdStage, jobs.data(), jobBytes);
+        std::memcpy(g_pdStage + offAt, offsets.data(), offBytes);
+        char *dBuf = nullptr;
+        if ((e = cudaMallocAsync((void **)&dBuf, cellAt + cellBytes, st))) return cuda_fail(e, "pd_resample_many jobs");
+        PdJob *dJobs = reinterpret_cast<PdJob *>(dBuf);
+        const int *dOff = reinterpret_cast<const int *>(dBuf + offAt);
+        float2 *dCells = reinterpret_cast<float2 *>(dBuf + cellAt);
+        if ((e = cudaMemcpyAsync(dBuf, g_pdStage, cellAt, cudaMemcpyHostToDevice, st)) ||
+            (e = cudaEventRecord(s0->ev0, st)) || (e = pd_launch_resample_many(dJobs, nj, st)) ||
+            (e = cudaEventRecord(s0->ev1, st)) || (e = pd_launch_gather_regions(dJobs, dOff, nj, dCells, st)) ||
+            (e = cudaMemcpyAsync(g_pdStage + cellAt, dCells, cellBytes, cudaMemcpyDeviceToHost, st))) {
+            cudaFreeAsync(dBuf, st);
+            cudaStreamSynchronize(st);
             return cuda_fail(e, "pd_resample_many");
         }
-        for (size_t k = 0; k < jobs.size(); ++k) {
+        cudaFreeAsync(dBuf, st);
+        if ((e = cudaStreamSynchronize(st))) return cuda_fail(e, "pd_resample_many read");
+        const float2 *packed = reinterpret_cast<const float2 *>(g_pdStage + cellAt);
+        for (int k = 0; k < nj; ++k) {
             pd_sampler *s = samplers[jobOf[k]];
             const PdJob &j = jobs[k];
             s->roundBase += (unsigned)s->trials;
-            size_t pitch = (size_t)s->gridW * sizeof(float2), off = (size_t)j.y0 * s->gridW + j.x0;
-            if ((e = cudaMemcpy2DAsync(s->cells.data() + off, pitch, s->grid.p + off, pitch,
-                                       (j.x1 - j.x0) * sizeof(float2), j.y1 - j.y0, cudaMemcpyDeviceToHost, st)))
-                break;
+            int w = j.x1 - j.x0;
+            for (int y = j.y0; y < j.y1; ++y)
+                std::memcpy(s->cells.data() + (size_t)y * s->gridW + j.x0, packed + offsets[k] + (y - j.y0) * w,
+                            sizeof(float2) * w);
         }
-        cudaFreeAsync(dJobs, st);
-        cudaError_t e2 = cudaStreamSynchronize(st);
-        if (e || (e = e2)) return cuda_fail(e, "pd_resample_many read");
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, s0->ev0, s0->ev1);
         total += ms;
