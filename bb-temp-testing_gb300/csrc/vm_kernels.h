@@ -107,4 +107,7 @@ cudaError_t pd_launch_gather_regions(const PdJob *jobs, const int *offsets, int 
 // 1 when the region runs as one block (every phase in one pass of it).
 int pd_small_region(int x0, int y0, int x1, int y1);
 // Small regions of distinct samplers (jobs in device memory), one block each.
-cudaError_t pd_launch_resample_many(const PdJob *jobs, int n, cudaStream_t s);
+// stageBytes: the largest pd_stage_bytes among the jobs' regions (the staged
+// region and halo size the launch's shared memory).
+size_t pd_stage_bytes(int x0, int y0, int x1, int y1);
+cudaError_t pd_launch_resample_many(const PdJob *jobs, int n, size_t stageBytes, cudaStream_t s);

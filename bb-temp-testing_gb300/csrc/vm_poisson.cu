@@ -92,41 +92,82 @@ __global__ void __launch_bounds__(256) k_phase(float2 *grid, PdParams p, int x0,
 // A whole resample of a small region in one block: the clear, then every
 // round's 9 phases separated by block barriers (the same order as the
 // one-launch-per-phase path, so the same samples). It replaces 1 + 9 x trials
-// launches by one when every phase fits in one pass of the block.
+// launches by one when every phase fits in one pass of the block. The region
+// and its 2-cell halo are staged in shared memory for all the phases (the
+// halo is only read: no dart outside the region is thrown), and the region
+// is written back at the end.
 constexpr int kSmallBlock = 1024;
+// The largest staged region: (3a + 4)(3b + 4) cells for ab <= kSmallBlock
+// phase cells, at most 21,532 (a = 1, b = 1024), as float2.
+constexpr int kMaxStageBytes = 21532 * 8;
+
+// One dart (dart above) against the staged copy: s holds the cells of the
+// rectangle at (hx0, hy0) with row length lw.
+__device__ __forceinline__ void dart_staged(float2 *s, int lw, int hx0, int hy0, const PdParams &p, int cx, int cy,
+                                            unsigned keyX, unsigned keyY)
+{
+    int li = (cy - hy0) * lw + (cx - hx0);
+    if (s[li].x >= 0.0f) return;
+    int cellId = cy * p.gridW + cx;
+    float x = ((float)cx + prand01((unsigned)cellId, keyX)) * p.cellSize;
+    float y = ((float)cy + prand01((unsigned)cellId, keyY)) * p.cellSize;
+    if (x >= p.width || y >= p.height) return;
+    float r2 = p.radius * p.radius;
+#pragma unroll 4
+    for (int k = 0; k < 24; ++k) {
+        int nx = cx + kRingDx[k], ny = cy + kRingDy[k];
+        if (nx < 0 || nx >= p.gridW || ny < 0 || ny >= p.gridH) continue;
+        float2 q = s[li + kRingDy[k] * lw + kRingDx[k]];
+        if (q.x < 0.0f) continue;
+        float dx = q.x - x, dy = q.y - y;
+        if (dx * dx + dy * dy < r2) return;
+    }
+    s[li] = make_float2(x, y);
+}
 
 __device__ __forceinline__ void resample_block(float2 *grid, const PdParams &p, int x0, int y0, int x1, int y1,
-                                               int trials, unsigned roundBase)
+                                               int trials, unsigned roundBase, float2 *s)
 {
-    int rw = x1 - x0, n = rw * (y1 - y0);
-    for (int t = threadIdx.x; t < n; t += blockDim.x)
-        grid[(size_t)(y0 + t / rw) * p.gridW + x0 + t % rw] = make_float2(-1.0f, -1.0f);
+    int rw = x1 - x0, rh = y1 - y0, lw = rw + 4, lh = rh + 4, hx0 = x0 - 2, hy0 = y0 - 2;
+    // the region cleared, the halo copied (cells outside the grid stay empty)
+    for (int t = threadIdx.x; t < lw * lh; t += blockDim.x) {
+        int gx = hx0 + t % lw, gy = hy0 + t / lw;
+        bool region = gx >= x0 && gx < x1 && gy >= y0 && gy < y1;
+        bool inGrid = gx >= 0 && gx < p.gridW && gy >= 0 && gy < p.gridH;
+        s[t] = !region && inGrid ? grid[(size_t)gy * p.gridW + gx] : make_float2(-1.0f, -1.0f);
+    }
     __syncthreads();
     for (int round = 0; round < trials; ++round) {
         unsigned r = roundBase + (unsigned)round;
         unsigned kx = round_key(r, p.seed, 0u), ky = round_key(r, p.seed, 1u);
         for (int py = 0; py < 3; ++py)
             for (int px = 0; px < 3; ++px) {
-                int tw = (x1 - x0 - px + 2) / 3, th = (y1 - y0 - py + 2) / 3;
+                int tw = (rw - px + 2) / 3, th = (rh - py + 2) / 3;
                 for (int t = threadIdx.x; t < tw * th; t += blockDim.x)
-                    dart(grid, p, x0 + 3 * (t % tw) + px, y0 + 3 * (t / tw) + py, kx, ky);
+                    dart_staged(s, lw, hx0, hy0, p, x0 + 3 * (t % tw) + px, y0 + 3 * (t / tw) + py, kx, ky);
                 __syncthreads(); // the next phase sees this phase's samples
             }
+    }
+    for (int t = threadIdx.x; t < rw * rh; t += blockDim.x) {
+        int lx = t % rw, ly = t / rw;
+        grid[(size_t)(y0 + ly) * p.gridW + x0 + lx] = s[(ly + 2) * lw + lx + 2];
     }
 }
 
 __global__ void __launch_bounds__(kSmallBlock) k_resample_block(float2 *grid, PdParams p, int x0, int y0, int x1,
                                                                  int y1, int trials, unsigned roundBase)
 {
-    resample_block(grid, p, x0, y0, x1, y1, trials, roundBase);
+    extern __shared__ float2 sStage[];
+    resample_block(grid, p, x0, y0, x1, y1, trials, roundBase, sStage);
 }
 
 // Many samplers' small regions in one launch, one block each (the samplers'
 // grids are disjoint, so the blocks are independent).
 __global__ void __launch_bounds__(kSmallBlock) k_resample_many(const PdJob *__restrict__ jobs)
 {
+    extern __shared__ float2 sStage[];
     PdJob j = jobs[blockIdx.x];
-    resample_block(j.grid, j.p, j.x0, j.y0, j.x1, j.y1, j.trials, j.roundBase);
+    resample_block(j.grid, j.p, j.x0, j.y0, j.x1, j.y1, j.trials, j.roundBase, sStage);
 }
 
 // The cells of each job's region, packed row by row at out + offsets[job]
@@ -154,6 +195,22 @@ cudaError_t pd_launch_gather_regions(const PdJob *jobs, const int *offsets, int 
     return cudaGetLastError();
 }
 
+// The one-block resamples stage up to kMaxStageBytes of shared memory (set
+// once per device).
+static cudaError_t stage_attributes()
+{
+    static bool done[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_resample_block, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes)) ||
+        (e = cudaFuncSetAttribute(k_resample_many, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes)))
+        return e;
+    if (dev >= 0 && dev < 64) done[dev] = true;
+    return cudaSuccess;
+}
+
 cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1, int y1, int trials,
                                unsigned roundBase, cudaStream_t s, bool dependentLaunch)
 {
@@ -162,7 +219,10 @@ cudaError_t pd_launch_resample(float2 *grid, PdParams p, int x0, int y0, int x1,
     long long cells = (long long)rw * rh;
     long long phaseCells = (long long)((rw + 2) / 3) * ((rh + 2) / 3);
     if (phaseCells <= kSmallBlock) {
-        k_resample_block<<<1, kSmallBlock, 0, s>>>(grid, p, x0, y0, x1, y1, trials, roundBase);
+        cudaError_t e = stage_attributes();
+        if (e) return e;
+        size_t smem = pd_stage_bytes(x0, y0, x1, y1);
+        k_resample_block<<<1, kSmallBlock, smem, s>>>(grid, p, x0, y0, x1, y1, trials, roundBase);
         return cudaGetLastError();
     }
     int cb = (int)((cells + 255) / 256);
@@ -197,9 +257,17 @@ int pd_small_region(int x0, int y0, int x1, int y1)
     return x1 > x0 && y1 > y0 && phaseCells <= kSmallBlock;
 }
 
-cudaError_t pd_launch_resample_many(const PdJob *jobs, int n, cudaStream_t s)
+size_t pd_stage_bytes(int x0, int y0, int x1, int y1)
+{
+    return sizeof(float2) * (size_t)(x1 - x0 + 4) * (size_t)(y1 - y0 + 4);
+}
+
+cudaError_t pd_launch_resample_many(const PdJob *jobs, int n, size_t stageBytes, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    k_resample_many<<<n, kSmallBlock, 0, s>>>(jobs);
+    if (stageBytes > (size_t)kMaxStageBytes) return cudaErrorInvalidValue;
+    cudaError_t e = stage_attributes();
+    if (e) return e;
+    k_resample_many<<<n, kSmallBlock, stageBytes, s>>>(jobs);
     return cudaGetLastError();
 }

@@ -1490,6 +1490,8 @@ int pd_resample_many(pd_sampler *const *samplers, const int *regions, int n, flo
         cudaStream_t st = s0->stream;
         // the regions come back packed: one device-to-host copy for all of them
         int nj = (int)jobs.size();
+        size_t stageBytes = 0;
+        for (const PdJob &j : jobs) stageBytes = std::max(stageBytes, pd_stage_bytes(j.x0, j.y0, j.x1, j.y1));
         std::vector<int> offsets(nj + 1, 0);
         for (int k = 0; k < nj; ++k)
             offsets[k + 1] = offsets[k] + (jobs[k].x1 - jobs[k].x0) * (jobs[k].y1 - jobs[k].y0);
@@ -1513,7 +1515,7 @@ int pd_resample_many(pd_sampler *const *samplers, const int *regions, int n, flo
         const int *dOff = reinterpret_cast<const int *>(dBuf + offAt);
         float2 *dCells = reinterpret_cast<float2 *>(dBuf + cellAt);
         if ((e = cudaMemcpyAsync(dBuf, g_pdStage, cellAt, cudaMemcpyHostToDevice, st)) ||
-            (e = cudaEventRecord(s0->ev0, st)) || (e = pd_launch_resample_many(dJobs, nj, st)) ||
+            (e = cudaEventRecord(s0->ev0, st)) || (e = pd_launch_resample_many(dJobs, nj, stageBytes, st)) ||
             (e = cudaEventRecord(s0->ev1, st)) || (e = pd_launch_gather_regions(dJobs, dOff, nj, dCells, st)) ||
             (e = cudaMemcpyAsync(g_pdStage + cellAt, dCells, cellBytes, cudaMemcpyDeviceToHost, st))) {
             cudaFreeAsync(dBuf, st);
