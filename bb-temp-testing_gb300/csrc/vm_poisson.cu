@@ -101,28 +101,32 @@ constexpr int kSmallBlock = 1024;
 // phase cells, at most 21,532 (a = 1, b = 1024), as float2.
 constexpr int kMaxStageBytes = 21532 * 8;
 
-// One dart (dart above) against the staged copy: s holds the cells of the
-// rectangle at (hx0, hy0) with row length lw.
+// One dart (dart above) against the staged copy, tested by a group of 4
+// lanes (gmask: the group's lanes of the warp, all active together; sub: this
+// lane's place in it). s holds the cells of the rectangle at (hx0, hy0) with
+// row length lw; every neighbour of a region cell lies in it, and cells
+// outside the grid hold the empty marker, so no bounds test is needed. Each
+// lane tests 6 of the 24 neighbours; the dart lands if no lane finds a
+// conflict, which does not depend on the order of the tests.
 __device__ __forceinline__ void dart_staged(float2 *s, int lw, int hx0, int hy0, const PdParams &p, int cx, int cy,
-                                            unsigned keyX, unsigned keyY)
+                                            unsigned keyX, unsigned keyY, int sub, unsigned gmask)
 {
     int li = (cy - hy0) * lw + (cx - hx0);
-    if (s[li].x >= 0.0f) return;
     int cellId = cy * p.gridW + cx;
     float x = ((float)cx + prand01((unsigned)cellId, keyX)) * p.cellSize;
     float y = ((float)cy + prand01((unsigned)cellId, keyY)) * p.cellSize;
-    if (x >= p.width || y >= p.height) return;
+    bool ok = s[li].x < 0.0f && x < p.width && y < p.height; // the same for the group
     float r2 = p.radius * p.radius;
-#pragma unroll 4
-    for (int k = 0; k < 24; ++k) {
-        int nx = cx + kRingDx[k], ny = cy + kRingDy[k];
-        if (nx < 0 || nx >= p.gridW || ny < 0 || ny >= p.gridH) continue;
-        float2 q = s[li + kRingDy[k] * lw + kRingDx[k]];
-        if (q.x < 0.0f) continue;
-        float dx = q.x - x, dy = q.y - y;
-        if (dx * dx + dy * dy < r2) return;
+    bool hit = false;
+    if (ok) {
+#pragma unroll
+        for (int k = sub; k < 24; k += 4) {
+            float2 q = s[li + kRingDy[k] * lw + kRingDx[k]];
+            float dx = q.x - x, dy = q.y - y;
+            hit |= q.x >= 0.0f && dx * dx + dy * dy < r2;
+        }
     }
-    s[li] = make_float2(x, y);
+    if (__ballot_sync(gmask, hit) == 0u && ok && sub == 0) s[li] = make_float2(x, y);
 }
 
 __device__ __forceinline__ void resample_block(float2 *grid, const PdParams &p, int x0, int y0, int x1, int y1,
@@ -143,8 +147,13 @@ __device__ __forceinline__ void resample_block(float2 *grid, const PdParams &p, 
         for (int py = 0; py < 3; ++py)
             for (int px = 0; px < 3; ++px) {
                 int tw = (rw - px + 2) / 3, th = (rh - py + 2) / 3;
-                for (int t = threadIdx.x; t < tw * th; t += blockDim.x)
-                    dart_staged(s, lw, hx0, hy0, p, x0 + 3 * (t % tw) + px, y0 + 3 * (t / tw) + py, kx, ky);
+                // 4 lanes per dart: the groups are aligned 4-lane slices of a warp
+                unsigned gmask = 0xFu << (threadIdx.x & 28u);
+                for (int t = threadIdx.x; t < 4 * tw * th; t += blockDim.x) {
+                    int d = t >> 2;
+                    dart_staged(s, lw, hx0, hy0, p, x0 + 3 * (d % tw) + px, y0 + 3 * (d / tw) + py, kx, ky, t & 3,
+                                gmask);
+                }
                 __syncthreads(); // the next phase sees this phase's samples
             }
     }
