@@ -48,14 +48,29 @@ __device__ __forceinline__ void dart(float2 *grid, const PdParams &p, int cx, in
     float r2 = p.radius * p.radius;
     // the 24 neighbours nearest first, so most rejected darts stop early (the
     // dart lands only if none conflicts, whatever the order)
+    if (cx >= 2 && cy >= 2 && cx < p.gridW - 2 && cy < p.gridH - 2) {
+        // an interior cell: every neighbour is in the grid; the offsets fold
+        // to constants in the unrolled loop
+        const int dxs[24] = {0, -1, 1, 0, -1, 1, -1, 1, 0, -2, 2, 0, -1, 1, -2, 2, -2, 2, -1, 1, -2, 2, -2, 2};
+        const int dys[24] = {-1, 0, 0, 1, -1, -1, 1, 1, -2, 0, 0, 2, -2, -2, -1, -1, 1, 1, 2, 2, -2, -2, 2, 2};
+        const float2 *c = grid + cellId;
+#pragma unroll
+        for (int k = 0; k < 24; ++k) {
+            float2 q = c[dys[k] * p.gridW + dxs[k]];
+            if (q.x < 0.0f) continue;
+            float dx = q.x - x, dy = q.y - y;
+            if (dx * dx + dy * dy < r2) return;
+        }
+    } else {
 #pragma unroll 4
-    for (int k = 0; k < 24; ++k) {
-        int nx = cx + kRingDx[k], ny = cy + kRingDy[k];
-        if (nx < 0 || nx >= p.gridW || ny < 0 || ny >= p.gridH) continue;
-        float2 q = grid[ny * p.gridW + nx];
-        if (q.x < 0.0f) continue;
-        float dx = q.x - x, dy = q.y - y;
-        if (dx * dx + dy * dy < r2) return;
+        for (int k = 0; k < 24; ++k) {
+            int nx = cx + kRingDx[k], ny = cy + kRingDy[k];
+            if (nx < 0 || nx >= p.gridW || ny < 0 || ny >= p.gridH) continue;
+            float2 q = grid[ny * p.gridW + nx];
+            if (q.x < 0.0f) continue;
+            float dx = q.x - x, dy = q.y - y;
+            if (dx * dx + dy * dy < r2) return;
+        }
     }
     grid[cellId] = make_float2(x, y);
 }
