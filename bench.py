@@ -107,6 +107,34 @@ def measured_peaks():
 # is a recorded figure, not measured by this run.
 K_LOSS_TRAFFIC = {"bytes_per_launch": 71845632,
                   "source": "ncu capture of k_loss<256,3> at the 1M-site workload, 2026-12-04 build"}
+# Warp instructions of one k_loss launch at this workload (smsp__inst_executed.sum)
+# from the same capture: the kernel is bound by instruction issue, and this
+# count against the GPU's issue rate (one warp instruction per scheduler and
+# cycle) shows how close it runs to that bound.
+K_LOSS_INSTRUCTIONS = {"warp_instructions_per_launch": 262.7e6,
+                       "source": "ncu capture of k_loss<256,3> at the 1M-site workload, 2026-12-04 build"}
+
+
+def issue_roofline(loss_ms: float, clocks: dict) -> dict:
+    """k_loss against the instruction-issue rate: its recorded warp
+    instructions per launch over the live mean launch time, against 4 warp
+    instructions per SM and cycle at the SM clock sampled in the run."""
+    sms = cuda_sm_count()
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    inst = K_LOSS_INSTRUCTIONS["warp_instructions_per_launch"]
+    if not (sms and mhz and loss_ms > 0):
+        return {"bound": "issue", "kernel": "k_loss", "achieved": None, "unavailable": "no SM count or clock"}
+    achieved = inst / (loss_ms / 1e3)
+    peak = 4.0 * sms * mhz * 1e6
+    return {"bound": "issue", "kernel": "k_loss", "achieved": achieved, "peak": peak,
+            "unit": "warp instructions/s", "frac": achieved / peak, "instructions_per_launch": inst,
+            "instructions_source": K_LOSS_INSTRUCTIONS["source"], "sms": sms, "sm_mhz": mhz}
+
+
+def cuda_sm_count() -> int:
+    import torch
+
+    return int(torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count)
 
 
 class ClockSampler:
@@ -741,6 +769,7 @@ def main():
                "sample": f"{steps} full steps of the 1M-site fit ({dt:.1f} s on {nthreads} threads)"}
 
     if rank == 0:
+        clk_summary = clk.summary()
         line = {
             "metric": METRIC, "value": value, "unit": "site-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps,
@@ -760,12 +789,13 @@ def main():
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": K_LOSS_TRAFFIC["bytes_per_launch"], "traffic_source": K_LOSS_TRAFFIC["source"],
                          "algorithmic_bytes_per_launch": lossBytes, "mean_launch_ms": loss_ms},
+            "issue_roofline": issue_roofline(loss_ms, clk_summary),
             # the whole step against HBM: B_step = 88 B per site + 8 B per target + 8 B per cell
             "step_roofline": {"bytes_per_step": stepBytes, "achieved": stepBytes / (ms / args.steps) / 1e6,
                               "unit": "GB/s", "frac": stepBytes / (ms / args.steps) / 1e6 / peak},
             "cpu_baseline": cpu,
             "fits": fits,
-            "clocks": clk.summary(),
+            "clocks": clk_summary,
             "gpu_launches": KERNELS_PER_STEP * args.steps,
         }
         print(json.dumps(line), flush=True)
