@@ -59,7 +59,8 @@ def parse():
                     help="--impl reference: cap on the timed CPU work (full steps of the whole fit)")
     ap.add_argument("--no-fits", action="store_true",
                     help="default workload: leave out the uneven-batch and served-stream figures")
-    ap.add_argument("--workload", default="scale", choices=["scale", "plain", "batch", "serve", "extract", "edit", "poisson", "canvas"],
+    ap.add_argument("--workload", default="scale", choices=["scale", "plain", "batch", "serve", "extract", "edit", "poisson", "canvas",
+                                                        "knn"],
                     help="scale: the 1M-site fit (the headline line); plain: the 2,048-site fit; batch / serve: fits/s workloads; "
                          "extract: the cell clipper; edit: the local-edit pipeline; poisson: the sampler; "
                          "canvas: RasterizeShape and StampDisc")
@@ -406,6 +407,52 @@ def run_extract(args):
                       "value": out["scale_1m"]["cells_per_s"], "workloads": out, "data": "synthetic"}), flush=True)
 
 
+def run_knn(args):
+    """The exact kNN query operator (reference knn<K>, voro_optimizer.cu:130-163)
+    on the 1M-site grid: 1,048,576 query points (a seeded subset of the
+    ellipse-union targets), K = 16, through VoroOptimizer.Knn (the queries
+    copied up, the sorted lists copied back: wall time of the call, best of
+    3), against the CPU oracle's kNN of a 20,000-query sample (1 thread and
+    all host threads); the GPU lists of that sample equal the oracle's."""
+    import voromesh_gb300 as vm
+    from voromesh_gb300 import synth
+    from oracle import oracle as orc
+
+    s = vm.Sampler(2.0, 2.0, RADIUS, 30, 1)
+    cells = s.Cells()
+    s.close()
+    spec = make_inputs(cells)
+    q = np.ascontiguousarray(spec.targets[synth.subset(5, 7, len(spec.targets), 1 << 20)])
+    K = 16
+    o = vm.VoroOptimizer(spec.width, spec.height, spec.spacing, vm.OptimizerParams(lossK=K))
+    o.SetGenerators(spec.generators, spec.slotsW, spec.slotsH, spec.slotCellSize)
+    o.Knn(q[:1024], K)  # warm-up
+    walls = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        idx, d2 = o.Knn(q, K)
+        walls.append(time.perf_counter() - t0)
+    o.close()
+    wall = min(walls)
+    sample = q[:20000]
+    gw = int(np.ceil(spec.width / spec.spacing))
+    grid = orc.Grid(spec.generators, gw, gw, spec.spacing)
+    t0 = time.perf_counter()
+    ridx, rd2 = grid.knn(sample, K, 1)
+    cpu1 = time.perf_counter() - t0
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    grid.knn(sample, K, nthreads)
+    cpuN = time.perf_counter() - t0
+    same = bool(np.array_equal(idx[:20000], ridx) and np.array_equal(d2[:20000].view(np.uint32), rd2.view(np.uint32)))
+    print(json.dumps({"metric": "queries/s, exact kNN (K=16) over the 1M-site grid", "unit": "queries/s",
+                      "value": len(q) / wall, "queries": len(q), "k": K, "wall_ms": wall * 1e3,
+                      "bytes_copied": int(q.nbytes + idx.nbytes + d2.nbytes),
+                      "cpu_baseline": {"value_1_thread": len(sample) / cpu1, "value_all_threads": len(sample) / cpuN,
+                                       "cores": nthreads, "kind": "port", "sample": f"{len(sample)} of the queries"},
+                      "bit_exact_vs_oracle_on_sample": same, "data": "synthetic"}), flush=True)
+
+
 def run_edit(args):
     """The local-edit pipeline of the reference's editor (Editor::Stamp,
     apps/voromesh_demo.cpp:117-156) with its defaults: a 1024 x 1024 domain,
@@ -678,6 +725,9 @@ def main():
         return
     if args.workload == "canvas":
         run_canvas(args)
+        return
+    if args.workload == "knn":
+        run_knn(args)
         return
     import torch
 

@@ -80,6 +80,7 @@ def lib() -> C.CDLL:
         _lib.vo_build_grid.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p]
         _lib.vo_knn.argtypes = [C.c_void_p, VoF2, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.vo_knn_many.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
         _lib.vo_knn_brute.argtypes = [C.c_void_p, C.c_int, VoF2, C.c_int, C.c_void_p, C.c_void_p]
         _lib.vo_loss_detail.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_float,
                                         C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -159,14 +160,11 @@ class Grid:
         self.spos = np.ascontiguousarray(self.spos)
         self.c = VoGrid(gw, gh, cell, P(self.start).value, P(self.sidx).value, P(self.spos).value)
 
-    def knn(self, queries: np.ndarray, K: int):
+    def knn(self, queries: np.ndarray, K: int, nthreads: int = 1):
         q = np.ascontiguousarray(queries, np.float32)
         idx = np.empty((len(q), K), np.int32)
         d2 = np.empty((len(q), K), np.float32)
-        L = lib()
-        for i in range(len(q)):
-            L.vo_knn(C.byref(self.c), VoF2(q[i, 0], q[i, 1]), K, C.c_void_p(idx[i].ctypes.data),
-                     C.c_void_p(d2[i].ctypes.data))
+        lib().vo_knn_many(C.byref(self.c), P(q), len(q), K, P(idx), P(d2), nthreads)
         return idx, d2
 
     def cells(self, width: float, height: float, masks=None, tilesX=0, tilesY=0, invVoxel=0.0, nthreads=1):

@@ -182,6 +182,27 @@ void vo_knn(const vo_grid *g, vo_f2 q, int K, int *idx, float *d2)
     }
 }
 
+typedef struct {
+    const vo_grid *g;
+    const vo_f2 *q;
+    int K;
+    int *idx;
+    float *d2;
+} knn_job;
+
+static void knn_range(void *ctx, int64_t lo, int64_t hi, int tid)
+{
+    (void)tid;
+    knn_job *J = (knn_job *)ctx;
+    for (int64_t i = lo; i < hi; ++i) vo_knn(J->g, J->q[i], J->K, J->idx + i * J->K, J->d2 + i * J->K);
+}
+
+void vo_knn_many(const vo_grid *g, const vo_f2 *q, int n, int K, int *idx, float *d2, int nthreads)
+{
+    knn_job J = {g, q, K, idx, d2};
+    vo_parallel(nthreads, n, knn_range, &J);
+}
+
 void vo_knn_brute(const vo_f2 *gen, int n, vo_f2 q, int K, int *idx, float *d2)
 {
     for (int k = 0; k < K; ++k) {

@@ -70,6 +70,8 @@ void vo_build_grid(const vo_f2 *gen, int n, int gw, int gh, float cellSize, int 
 /* ---- kNN ------------------------------------------------------------------ */
 /* knn<K> ring search (voro_optimizer.cu:130-163); ties ordered by site index. */
 void vo_knn(const vo_grid *g, vo_f2 q, int K, int *idx, float *d2);
+/* vo_knn for n queries (row i of idx / d2 for query i), split over nthreads threads. */
+void vo_knn_many(const vo_grid *g, const vo_f2 *q, int n, int K, int *idx, float *d2, int nthreads);
 /* Exhaustive K nearest by (d2, index) over all live slots (a test aid). */
 void vo_knn_brute(const vo_f2 *gen, int n, vo_f2 q, int K, int *idx, float *d2);
 
