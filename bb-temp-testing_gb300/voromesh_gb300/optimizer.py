@@ -250,10 +250,20 @@ class VoroOptimizer:
         check(self._lib.vm_get_grid(self._h, None, ptr(sidx), ptr(spos), None), "Grid")
         return start, sidx, spos, genCell
 
-    def Knn(self, queries, K: int):
+    def Knn(self, queries, K: int, out=None):
+        """The K nearest sites of each query (indices, squared distances).
+        `out` = (idx, d2), int32 and float32 arrays of shape (n, K), are
+        filled in place of new arrays (a caller reusing them skips the page
+        faults of fresh output memory)."""
         q = _pts(queries, "queries")
-        idx = np.empty((len(q), K), np.int32)
-        d2 = np.empty((len(q), K), np.float32)
+        if out is None:
+            idx = np.empty((len(q), K), np.int32)
+            d2 = np.empty((len(q), K), np.float32)
+        else:
+            idx, d2 = out
+            if (idx.shape != (len(q), K) or d2.shape != (len(q), K) or idx.dtype != np.int32
+                    or d2.dtype != np.float32 or not idx.flags.c_contiguous or not d2.flags.c_contiguous):
+                raise ValueError("out must be C-contiguous int32 and float32 arrays of shape (n, K)")
         check(self._lib.vm_knn(self._h, ptr(q), len(q), K, ptr(idx), ptr(d2)), "Knn")
         return idx, d2
 

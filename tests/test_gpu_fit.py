@@ -91,6 +91,13 @@ def test_knn_bit_exact(vm, orc, K):
     ridx, rd2 = grid.knn(q, K)
     assert np.array_equal(idx, ridx)
     assert np.array_equal(d2, rd2)
+    # the caller's own output arrays, filled in place
+    out = (np.full((len(q), K), -7, np.int32), np.full((len(q), K), -7.0, np.float32))
+    i2, e2 = opt.Knn(q, K, out=out)
+    assert i2 is out[0] and e2 is out[1]
+    assert np.array_equal(out[0], ridx) and np.array_equal(out[1], rd2)
+    with pytest.raises(ValueError):
+        opt.Knn(q, K, out=(out[0][:, :K - 1], out[1]))
 
 
 def test_probe_matches_oracle(vm, orc):
