@@ -6,6 +6,9 @@
 //   k_loss        warp-staged 5x5 cell blocks with certificates; uncertain
 //                 targets go to a queue
 //   k_loss_exact  the queued targets: exact ring search, one per thread
+//   k_small_grid  the rest of a small fit's step in one block: the queued
+//                 targets and Adam schedule, Adam, binning, scan, scatter
+//                 (here beside k_loss_exact, whose pass it runs first)
 #include "vm_device.cuh"
 #include "vm_adam.cuh"
 #include "vm_knn.cuh"
