@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(1024) k_scan3_single(int *a, int *b, int *c, i
 // ---------------------------------------------------------------------------
 // The samples of one voxel's run (record indices run[0..n)) summed in
 // double in sample order (canvas.cpp:13-25 adds them so): repeated selection
-// of the next sample index.
+// of the next sample index, for the short runs one lane reduces.
 __device__ __noinline__ void ordered_sum(const float4 *rec, const int *run, int n, double &sx, double &sy)
 {
     sx = 0.0;
@@ -246,6 +246,49 @@ __device__ __noinline__ void ordered_sum(const float4 *rec, const int *run, int 
     }
 }
 
+// Sorts a long run (record indices) by sample index in place, by the whole
+// warp: a bitonic network over the next power of two P >= n in which every
+// merge of two sorted blocks opens with the comparators (i, i ^ (k - 1)),
+// so that every comparator puts the smaller key first. A comparator whose
+// upper position is at or past n is skipped: that is the same network on
+// the run padded with +inf keys, which never move. log2(P) (log2(P) + 1) / 2
+// stages of P / 2 comparators, 32 a warp step; __syncwarp orders the
+// stages' global loads and stores.
+__device__ __noinline__ void warp_sort_run(const float4 *__restrict__ rec, int *run, int n)
+{
+    const int lane = threadIdx.x & 31;
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < (P >> 1); i += 32) {
+                const int a = ((i & ~(j - 1)) << 1) | (i & (j - 1)); // bit j of a is clear
+                const int b = j == (k >> 1) ? a ^ (k - 1) : a | j;
+                if (b < n) {
+                    const int ra = run[a], rb = run[b];
+                    if (__float_as_int(rec[rb].z) < __float_as_int(rec[ra].z)) {
+                        run[a] = rb;
+                        run[b] = ra;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// The same sum over a run already in sample order.
+__device__ __noinline__ void in_order_sum(const float4 *rec, const int *run, int n, double &sx, double &sy)
+{
+    sx = 0.0;
+    sy = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const float4 q = rec[run[k]];
+        sx += (double)q.x;
+        sy += (double)q.y;
+    }
+}
+
 // Split of a float into sign, integer significand M and exponent e with
 // |v| = M * 2^(e - 150) (e = 1 for subnormals).
 __device__ __forceinline__ void float_split(float v, bool &neg, unsigned &M, int &e)
@@ -258,7 +301,7 @@ __device__ __forceinline__ void float_split(float v, bool &neg, unsigned &M, int
     e = be > 0 ? be : 1;
 }
 
-// Exact mean of one voxel whose records are rec[perm[run[k]]], k < n.
+// Exact mean of one voxel whose records are rec[run[k]], k < n.
 // Every sample is an integer multiple of Q = 2^(e0 - 150), where e0 is the
 // smallest exponent among the tile's non-zero samples (per axis). When the
 // voxel's magnitudes sum to at most 2^52 Q, every partial sum of its samples
@@ -296,13 +339,21 @@ struct RunSums {
         add_axis(q.x, ex, sx, ax);
         add_axis(q.y, ey, sy, ay);
     }
-    __device__ float2 mean(const float4 *__restrict__ rec, const int *__restrict__ run, int n, int ex, int ey) const
+    __device__ bool exact() const
     {
         const unsigned long long lim = 1ull << 52;
+        return !big && ax <= lim && ay <= lim;
+    }
+    // sorted: the run is in sample order (a long run after warp_sort_run)
+    __device__ float2 mean(const float4 *__restrict__ rec, const int *__restrict__ run, int n, int ex, int ey,
+                           bool sorted) const
+    {
         double x, y;
-        if (!big && ax <= lim && ay <= lim) {
+        if (exact()) {
             x = ex == INT_MAX ? 0.0 : ldexp((double)sx, ex - 150);
             y = ey == INT_MAX ? 0.0 : ldexp((double)sy, ey - 150);
+        } else if (sorted) {
+            in_order_sum(rec, run, n, x, y);
         } else {
             ordered_sum(rec, run, n, x, y);
         }
@@ -314,13 +365,14 @@ __device__ float2 voxel_mean(const float4 *__restrict__ rec, const int *__restri
 {
     RunSums r;
     for (int k = 0; k < n; ++k) r.add(rec[run[k]], ex, ey);
-    return r.mean(rec, run, n, ex, ey);
+    return r.mean(rec, run, n, ex, ey, false);
 }
 
 // The same for a long run, by the whole warp: lanes take every 32nd sample
-// and the integer sums are combined exactly by shuffles. Returns the mean on
-// every lane.
-__device__ float2 voxel_mean_warp(const float4 *__restrict__ rec, const int *__restrict__ run, int n, int ex, int ey)
+// and the integer sums are combined exactly by shuffles; a run that fails
+// the exact-sum bound is sorted into sample order by the warp (its order in
+// run[] is otherwise arbitrary). Returns the mean on every lane.
+__device__ float2 voxel_mean_warp(const float4 *__restrict__ rec, int *run, int n, int ex, int ey)
 {
     const int lane = threadIdx.x & 31;
     RunSums r;
@@ -332,8 +384,9 @@ __device__ float2 voxel_mean_warp(const float4 *__restrict__ rec, const int *__r
         r.ay += __shfl_xor_sync(0xffffffffu, r.ay, o);
     }
     r.big = __any_sync(0xffffffffu, r.big);
+    if (!r.exact()) warp_sort_run(rec, run, n); // the sums are the warp's totals: a uniform branch
     float2 m = make_float2(0.0f, 0.0f);
-    if (lane == 0) m = r.mean(rec, run, n, ex, ey);
+    if (lane == 0) m = r.mean(rec, run, n, ex, ey, true);
     m.x = __shfl_sync(0xffffffffu, m.x, 0);
     m.y = __shfl_sync(0xffffffffu, m.y, 0);
     return m;

@@ -36,6 +36,16 @@ def shapes():
     # decide
     tiny = np.float32(1.5 * 2.0 ** -20)
     yield "wrap_voxel", (512.0, 512.0, 64.0), np.array([[tiny, tiny]] + [[288.0, 288.0]] * 7279, np.float32)
+    # 64 samples in voxel 0, one per vertex (every edge is shorter than the
+    # quarter-voxel step): 16 of 2^-50 and 48 summing to 64 + 2^-18, so the
+    # mean sits on a float rounding tie, 1 + 2^-24. Summed first, the small
+    # ones add 2^-52 to the mean, which rounds up to 1 + 2^-23; summed after
+    # the large ones, they vanish and the tie rounds to 1. The mean depends on
+    # the sample order, which the long-run fallback must restore.
+    lo = [[2.0 ** -50, 2.0 ** -50]] * 16
+    hi = [[1.0, 1.0]] * 46 + [[9.0, 9.0], [9.0 + 2.0 ** -18, 9.0 + 2.0 ** -18]]
+    yield "order_small_first", (512.0, 512.0, 64.0), np.array(lo + hi, np.float32)
+    yield "order_small_last", (512.0, 512.0, 64.0), np.array(hi + lo, np.float32)
 
 
 def shape(name):
@@ -44,4 +54,5 @@ def shape(name):
 
 # static, so that collecting the tests imports nothing of the package
 NAMES = ["heart_1k", "heart_small_domain", "odd_grid", "triangle_outside", "tiny_ring", "comb", "tiny_coords",
-         "single_vertex", "grid_aligned", "pentagram", "clockwise_square", "sliver", "random_poly", "wrap_voxel"]
+         "single_vertex", "grid_aligned", "pentagram", "clockwise_square", "sliver", "random_poly", "wrap_voxel",
+         "order_small_first", "order_small_last"]
