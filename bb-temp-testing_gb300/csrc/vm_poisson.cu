@@ -37,40 +37,71 @@ __device__ __forceinline__ float prand01(unsigned cell, unsigned key)
 __constant__ signed char kRingDx[24] = {0, -1, 1, 0, -1, 1, -1, 1, 0, -2, 2, 0, -1, 1, -2, 2, -2, 2, -1, 1, -2, 2, -2, 2};
 __constant__ signed char kRingDy[24] = {-1, 0, 0, 1, -1, -1, 1, 1, -2, 0, 0, 2, -2, -2, -1, -1, 1, 1, 2, 2, -2, -2, 2, 2};
 
+// True if any of the N staged neighbours (q.x < 0: an empty cell) is nearer
+// than r to the dart (x, y).
+template <int N>
+__device__ __forceinline__ bool any_conflict(const float2 (&q)[N], float x, float y, float r2)
+{
+    bool hit = false;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        float dx = q[k].x - x, dy = q[k].y - y;
+        hit |= q[k].x >= 0.0f && dx * dx + dy * dy < r2;
+    }
+    return hit;
+}
+
+// Neighbours of an interior cell loaded per batch (nearest first): the own
+// cell with the first kFirstBatch, then batches of kBatch.
+constexpr int kFirstBatch = 8, kBatch = 4;
+static_assert((24 - kFirstBatch) % kBatch == 0, "the rest splits into whole batches");
+
 // One dart for cell (cx, cy) (reference dartPhaseKernel :84-106).
 __device__ __forceinline__ void dart(float2 *grid, const PdParams &p, int cx, int cy, unsigned keyX, unsigned keyY)
 {
     int cellId = cy * p.gridW + cx;
+    float r2 = p.radius * p.radius;
+    if (cx >= 2 && cy >= 2 && cx < p.gridW - 2 && cy < p.gridH - 2) {
+        // an interior cell: every neighbour is in the grid, and no address
+        // depends on a loaded value, so the cell and its 8 nearest
+        // neighbours are loaded as one batch and the 16 at distance 2 as the
+        // next (the dart lands only if none conflicts, whatever the order)
+        const int dxs[24] = {0, -1, 1, 0, -1, 1, -1, 1, 0, -2, 2, 0, -1, 1, -2, 2, -2, 2, -1, 1, -2, 2, -2, 2};
+        const int dys[24] = {-1, 0, 0, 1, -1, -1, 1, 1, -2, 0, 0, 2, -2, -2, -1, -1, 1, 1, 2, 2, -2, -2, 2, 2};
+        const float2 *c = grid + cellId;
+        const int W = p.gridW;
+        float2 own = c[0];
+        float2 q1[kFirstBatch];
+#pragma unroll
+        for (int k = 0; k < kFirstBatch; ++k) q1[k] = c[dys[k] * W + dxs[k]];
+        if (own.x >= 0.0f) return;
+        float x = ((float)cx + prand01((unsigned)cellId, keyX)) * p.cellSize;
+        float y = ((float)cy + prand01((unsigned)cellId, keyY)) * p.cellSize;
+        if (x >= p.width || y >= p.height) return;
+        if (any_conflict(q1, x, y, r2)) return;
+#pragma unroll
+        for (int b = kFirstBatch; b < 24; b += kBatch) {
+            float2 q2[kBatch];
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) q2[k] = c[dys[b + k] * W + dxs[b + k]];
+            if (any_conflict(q2, x, y, r2)) return;
+        }
+        grid[cellId] = make_float2(x, y);
+        return;
+    }
     if (grid[cellId].x >= 0.0f) return;
     float x = ((float)cx + prand01((unsigned)cellId, keyX)) * p.cellSize;
     float y = ((float)cy + prand01((unsigned)cellId, keyY)) * p.cellSize;
     if (x >= p.width || y >= p.height) return;
-    float r2 = p.radius * p.radius;
-    // the 24 neighbours nearest first, so most rejected darts stop early (the
-    // dart lands only if none conflicts, whatever the order)
-    if (cx >= 2 && cy >= 2 && cx < p.gridW - 2 && cy < p.gridH - 2) {
-        // an interior cell: every neighbour is in the grid; the offsets fold
-        // to constants in the unrolled loop
-        const int dxs[24] = {0, -1, 1, 0, -1, 1, -1, 1, 0, -2, 2, 0, -1, 1, -2, 2, -2, 2, -1, 1, -2, 2, -2, 2};
-        const int dys[24] = {-1, 0, 0, 1, -1, -1, 1, 1, -2, 0, 0, 2, -2, -2, -1, -1, 1, 1, 2, 2, -2, -2, 2, 2};
-        const float2 *c = grid + cellId;
-#pragma unroll
-        for (int k = 0; k < 24; ++k) {
-            float2 q = c[dys[k] * p.gridW + dxs[k]];
-            if (q.x < 0.0f) continue;
-            float dx = q.x - x, dy = q.y - y;
-            if (dx * dx + dy * dy < r2) return;
-        }
-    } else {
+    // the 24 neighbours nearest first, so most rejected darts stop early
 #pragma unroll 4
-        for (int k = 0; k < 24; ++k) {
-            int nx = cx + kRingDx[k], ny = cy + kRingDy[k];
-            if (nx < 0 || nx >= p.gridW || ny < 0 || ny >= p.gridH) continue;
-            float2 q = grid[ny * p.gridW + nx];
-            if (q.x < 0.0f) continue;
-            float dx = q.x - x, dy = q.y - y;
-            if (dx * dx + dy * dy < r2) return;
-        }
+    for (int k = 0; k < 24; ++k) {
+        int nx = cx + kRingDx[k], ny = cy + kRingDy[k];
+        if (nx < 0 || nx >= p.gridW || ny < 0 || ny >= p.gridH) continue;
+        float2 q = grid[ny * p.gridW + nx];
+        if (q.x < 0.0f) continue;
+        float dx = q.x - x, dy = q.y - y;
+        if (dx * dx + dy * dy < r2) return;
     }
     grid[cellId] = make_float2(x, y);
 }
