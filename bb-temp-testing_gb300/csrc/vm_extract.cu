@@ -7,12 +7,15 @@
 // certifies the cell (|cj - ci|^2 > 4 max|v - ci|^2); an uncertified cell
 // falls back to every generator in index order, as in the reference.
 //
-// Arithmetic: each polygon vertex is the intersection of the lines of its two
-// edges, solved once in FP64 by a 2x2 determinant when the vertex is created
-// and kept in FP64 (and rounded to FP32). The inside/outside test of a vertex
+// Arithmetic: a new vertex is the reference's FP64 interpolation along the
+// clipped edge, t = fa / (fa - fb) with fa, fb the edge ends' signed
+// bisector values, each operation one IEEE rounding (built without FMA
+// contraction), so every vertex is the reference's bit for bit. Vertices are
+// kept in FP64 (and rounded to FP32). The inside/outside test of a vertex
 // against a new bisector runs in FP32 with a rigorous error bound and is
-// re-evaluated in FP64 only when the FP32 value lies inside that bound.
-// Centroid and output vertices use the FP64 vertices, as the reference does.
+// re-evaluated in FP64 only when the FP32 value lies inside that bound, which
+// gives the FP64 test's decision. Centroid and output vertices use the FP64
+// vertices, as the reference does.
 #include "vm_device.cuh"
 #include "vm_kernels.h"
 #include "vm_knn.cuh"
@@ -32,45 +35,7 @@ struct CellPoly {
 struct CellCtx {
     float2 ci;
     double w, h; // domain size
-    const float2 *gen;
 };
-
-// Line of an edge label in coordinates relative to ci: a . x = b.
-// label >= 0: bisector of ci and gen[label]; -1..-4: top, right, bottom, left box side.
-__device__ __forceinline__ void line_of(const CellCtx &c, int L, double &ax, double &ay, double &b)
-{
-    if (L >= 0) {
-        float2 g = c.gen[L];
-        double rx = (double)g.x - (double)c.ci.x, ry = (double)g.y - (double)c.ci.y;
-        ax = rx;
-        ay = ry;
-        b = 0.5 * (rx * rx + ry * ry);
-    } else if (L == -1) {
-        ax = 0.0; ay = 1.0; b = -(double)c.ci.y;
-    } else if (L == -2) {
-        ax = 1.0; ay = 0.0; b = c.w - (double)c.ci.x;
-    } else if (L == -3) {
-        ax = 0.0; ay = 1.0; b = c.h - (double)c.ci.y;
-    } else {
-        ax = 1.0; ay = 0.0; b = -(double)c.ci.x;
-    }
-}
-
-// Intersection of the line of label L with the bisector (rx, ry, cc).
-__device__ __forceinline__ void intersect(const CellCtx &c, int L, double rx, double ry, double cc, double fbx,
-                                          double fby, double &x, double &y)
-{
-    double ax, ay, b;
-    line_of(c, L, ax, ay, b);
-    double det = ax * ry - ay * rx;
-    if (det == 0.0) { // parallel: keep the edge point (cannot happen for a proper crossing)
-        x = fbx;
-        y = fby;
-        return;
-    }
-    x = (b * ry - cc * ay) / det;
-    y = (ax * cc - rx * b) / det;
-}
 
 // 1 if vertex k is outside the half-plane <x, r> <= |r|^2/2 (reference clipByBisector :322-325)
 __device__ __forceinline__ bool outside(const CellPoly &P, int k, float rfx, float rfy, float cf, double rx, double ry,
@@ -114,8 +79,11 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
             } else ok = false;
         }
         if (inA != inB) {
-            double x, y;
-            intersect(c, P.lab[k], rx, ry, cc, P.vx[k], P.vy[k], x, y);
+            // the reference's interpolation (:337-339); fa and fb differ in sign
+            const double ax = P.vx[k], ay = P.vy[k], bx = P.vx[k1], by = P.vy[k1];
+            const double fa = ax * rx + ay * ry - cc, fb = bx * rx + by * ry - cc;
+            const double t = fa / (fa - fb);
+            const double x = ax + t * (bx - ax), y = ay + t * (by - ay);
             if (Q.n < kMaxVerts) {
                 Q.vx[Q.n] = x; Q.vy[Q.n] = y;
                 Q.fx[Q.n] = (float)x; Q.fy[Q.n] = (float)y;
@@ -176,15 +144,26 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
         outInside[i] = 0;
         return;
     }
+    // the ring search keeps its top 32 in registers (every index a constant
+    // of the unrolled insertion); the clip loops below index the list at run
+    // time, which puts d2/idx in local memory, so they get one copy of it
     float d2[kCellK];
     int idx[kCellK];
-    knn_ring<kCellK>(F.start, F.sortedPos, F.sortedIdx, F.gridW, F.gridH, F.cell, F.inv, ci, d2, idx);
+    {
+        float rd2[kCellK];
+        int ridx[kCellK];
+        knn_ring<kCellK>(F.start, F.sortedPos, F.sortedIdx, F.gridW, F.gridH, F.cell, F.inv, ci, rd2, ridx);
+#pragma unroll
+        for (int k = 0; k < kCellK; ++k) {
+            d2[k] = rd2[k];
+            idx[k] = ridx[k];
+        }
+    }
 
     CellCtx c;
     c.ci = ci;
     c.w = (double)F.width;
     c.h = (double)F.height;
-    c.gen = F.gen;
     CellPoly buf[2];
     CellPoly *P = &buf[0], *Q = &buf[1];
     double x0 = -(double)ci.x, y0 = -(double)ci.y, x1 = c.w - (double)ci.x, y1 = c.h - (double)ci.y;

@@ -7,7 +7,8 @@
 - the 1M-site fit: the r = 1e-3 Poisson fill of [0,2]^2 (2829^2 cells), the
   1,048,576 generators drawn from it, 8,388,608 targets on the union of 64
   ellipses, k = 16: the fill, the whole grid, kNN lists and per-target
-  decisions on every 64th target, and three full steps;
+  decisions on every 64th target, three full steps, and the extraction of
+  the fitted sites (every cell and the boundary mesh);
 - the precision stress: a 512x512 lattice jittered by 1e-6 with 2,097,152
   targets on a 5-arm star, k = 16, ten steps, and the per-target decisions
   against the FP64 oracle's at the same positions.
@@ -101,6 +102,21 @@ def test_scale_fit_1m(vm, orc, fill_1e3):
         lref = ref.step(1)
         assert _same_state(opt, ref), f"after {step + 1} steps"
         assert np.float32(opt.LastBatchLoss()) == np.float32(lref)
+    # the cells of the fitted sites and their boundary mesh
+    from test_gpu_extract import assert_cells_equal, disc_masks
+
+    masks, tiles, voxel = disc_masks()
+    opt.SetOccupancy(masks, tiles, tiles, voxel)
+    mesh = opt.Extract()
+    gen = ref.generators()[0]
+    verts, edges, counts, inside, flags = orc.Grid(gen, gw, gw, spec.spacing).cells(
+        2.0, 2.0, masks, tiles, tiles, float(np.float32(1.0) / np.float32(voxel)), nthreads=THREADS)
+    assert np.array_equal(mesh.inside, inside) and inside.sum() > 100000
+    assert mesh.unsafeCells == flags[0] and mesh.overflowCells == flags[1]
+    assert_cells_equal(mesh, len(gen), verts, edges, counts)
+    _, mv, me, wt, loops = orc.assemble(verts, edges, counts, inside)
+    assert mesh.watertight == wt and mesh.loops == loops and np.array_equal(mesh.edges, me)
+    assert np.array_equal(mesh.vertices.view(np.uint32), mv.view(np.uint32))
 
 
 def test_precision_lattice_full_size(vm, orc):

@@ -1,10 +1,13 @@
 """GPU extraction parity: clipped Voronoi cells and the boundary mesh against
 the CPU oracle (the reference's FP64 clipper restated).
 
-Edge labels, vertex counts, cyclic order, occupancy and the unsafe/overflow
-counts must match exactly; vertex coordinates to FP32 rounding (the
-reference interpolates along the clipped edge in FP64, this library
-intersects the two edge lines in FP64; both round to float at the end).
+Edge labels, vertex counts, cyclic order, vertex coordinates, occupancy and
+the unsafe/overflow counts must match bit for bit: both sides clip with the
+reference's FP64 interpolation along the clipped edge, one IEEE rounding per
+operation, and the device's FP32 inside tests fall back to FP64 within their
+error bound, so they take the FP64 test's decisions. That includes the
+near-cocircular lattices, where any other arithmetic splits vertices
+differently.
 """
 import numpy as np
 import pytest
@@ -23,50 +26,30 @@ def disc_masks(tiles=16, radius=0.6):
     return masks, tiles, 2.0 / n
 
 
-def exact_cell(gen, i, order):
-    """The cell of site i clipped by the sites in `order`, in exact rational
-    arithmetic (labels per edge), for adjudicating near-degenerate cells."""
-    from fractions import Fraction as Fr
-
-    ci = [Fr(float(gen[i, 0])), Fr(float(gen[i, 1]))]
-    poly = [([-ci[0], -ci[1]], -1), ([2 - ci[0], -ci[1]], -2), ([2 - ci[0], 2 - ci[1]], -3), ([-ci[0], 2 - ci[1]], -4)]
-    for j in order:
-        if j == i or gen[j, 0] < 0:
-            continue
-        r = [Fr(float(gen[j, 0])) - ci[0], Fr(float(gen[j, 1])) - ci[1]]
-        c = (r[0] * r[0] + r[1] * r[1]) / 2
-        f = [v[0] * r[0] + v[1] * r[1] - c for v, _ in poly]
-        if not any(x > 0 for x in f):
-            continue
-        out = []
-        for k in range(len(poly)):
-            (a, ea), (b, _) = poly[k], poly[(k + 1) % len(poly)]
-            fa, fb = f[k], f[(k + 1) % len(poly)]
-            if fa <= 0:
-                out.append((a, ea))
-            if (fa <= 0) != (fb <= 0):
-                t = fa / (fa - fb)
-                out.append(([a[0] + t * (b[0] - a[0]), a[1] + t * (b[1] - a[1])], int(j) if fa <= 0 else ea))
-        poly = out
-    return [e for _, e in poly]
+def cell_table(mesh, n):
+    """The mesh's per-cell labels and vertices in fixed 24-wide rows."""
+    cs = np.asarray(mesh.cellStart)
+    cnt = np.diff(cs)
+    rows = np.repeat(np.arange(n), cnt)
+    cols = np.arange(cs[-1]) - np.repeat(cs[:-1], cnt)
+    lab = np.full((n, 24), -9999, np.int32)
+    ver = np.zeros((n, 24, 2), np.float32)
+    lab[rows, cols] = mesh.cellLabels
+    ver[rows, cols] = mesh.cellVerts
+    return cnt, lab, ver
 
 
-def drop_zero_edges(labels, verts):
-    """Removes edges whose two end vertices are the same float point."""
-    n = len(labels)
-    keep = [k for k in range(n) if not np.array_equal(verts[k], verts[(k + 1) % n])]
-    return [int(labels[k]) for k in keep]
+def assert_cells_equal(mesh, n, verts, edges, counts):
+    """Every cell equals the oracle's: count, labels and vertex bits."""
+    cnt, lab, ver = cell_table(mesh, n)
+    assert np.array_equal(cnt, counts)
+    used = np.arange(24)[None, :] < counts[:, None]
+    bad = ~np.all(np.where(used, edges, -9999) == lab, axis=1)
+    bad |= ~np.all(np.where(used[..., None], ver.view(np.uint32) == verts.view(np.uint32), True), axis=(1, 2))
+    assert not bad.any(), f"{int(bad.sum())} cells differ, first {np.flatnonzero(bad)[:8].tolist()}"
 
 
-def same_cycle(a, b):
-    if len(a) != len(b):
-        return False
-    if not a:
-        return True
-    return any(a[k:] + a[:k] == b for k in range(len(a)))
-
-
-def run_case(vm, orc, gen, spacing, tgt=None, degenerate=False):
+def run_case(vm, orc, gen, spacing, tgt=None):
     from voromesh_gb300 import OptimizerParams, VoroOptimizer
 
     n = len(gen)
@@ -81,30 +64,11 @@ def run_case(vm, orc, gen, spacing, tgt=None, degenerate=False):
     verts, edges, counts, inside, flags = grid.cells(2.0, 2.0, masks, tiles, tiles, float(np.float32(1.0) / np.float32(voxel)))
     assert np.array_equal(mesh.inside, inside)
     assert mesh.unsafeCells == flags[0] and mesh.overflowCells == flags[1]
-    adjudicated = 0
-    for i in range(n):
-        a, b = mesh.cellStart[i], mesh.cellStart[i + 1]
-        if b - a == counts[i] and np.array_equal(mesh.cellLabels[a:b], edges[i, :counts[i]]):
-            np.testing.assert_allclose(mesh.cellVerts[a:b], verts[i, :counts[i]], rtol=0, atol=5e-7)
-            continue
-        # The reference's FP64 interpolation can split a degenerate vertex into a
-        # zero-length edge; the same cell without such edges must match, or the
-        # library must agree with the exact rational cell.
-        assert degenerate, f"cell {i} differs"
-        mine = drop_zero_edges(mesh.cellLabels[a:b], mesh.cellVerts[a:b])
-        theirs = drop_zero_edges(edges[i, :counts[i]], verts[i, :counts[i]])
-        if not same_cycle(mine, theirs):
-            d = ((gen[:, 0].astype(np.float64) - gen[i, 0]) ** 2 + (gen[:, 1].astype(np.float64) - gen[i, 1]) ** 2)
-            exact = exact_cell(gen, i, np.argsort(d)[:48])
-            assert same_cycle(mine, exact), f"cell {i}: {mine} vs exact {exact}"
-        adjudicated += 1
-    if degenerate:
-        ref_watertight = orc.assemble(verts, edges, counts, inside)[3]
-        return mesh, adjudicated, ref_watertight
+    assert_cells_equal(mesh, n, verts, edges, counts)
     cs, mv, me, wt, loops = orc.assemble(verts, edges, counts, inside)
     assert mesh.watertight == wt and mesh.loops == loops
     assert np.array_equal(mesh.edges, me)
-    np.testing.assert_allclose(mesh.vertices, mv, rtol=0, atol=5e-7)
+    assert np.array_equal(mesh.vertices.view(np.uint32), mv.view(np.uint32))
     return mesh
 
 
@@ -118,18 +82,15 @@ def test_uniform_sites(vm, orc):
 
 
 def test_lattice_near_degenerate(vm, orc):
-    """Near-cocircular quadruples: a jittered lattice (the precision stress shape)."""
+    """Near-cocircular quadruples: a jittered lattice (the precision stress
+    shape). Per-cell clipping cannot keep vertex triples consistent across
+    cells there, so with 1e-6 jitter neither the reference's clipper nor this
+    one need be watertight; run_case checks that both give the same mesh."""
     from voromesh_gb300 import synth
 
-    gen = synth.lattice(5, 5, 48, 48, 1e-6)
-    mesh, adjudicated, ref_watertight = run_case(vm, orc, gen, 2.0 / 48, degenerate=True)
-    # per-cell clipping cannot keep vertex triples consistent across cells at
-    # near-cocircular quadruples; the reference's FP64 clipper is not
-    # watertight on this input either
-    assert mesh.watertight or not ref_watertight
-    gen = synth.lattice(5, 5, 48, 48, 1e-3)
-    mesh, _, ref_watertight = run_case(vm, orc, gen, 2.0 / 48, degenerate=True)
-    assert ref_watertight and mesh.watertight
+    run_case(vm, orc, synth.lattice(5, 5, 48, 48, 1e-6), 2.0 / 48)
+    mesh = run_case(vm, orc, synth.lattice(5, 5, 48, 48, 1e-3), 2.0 / 48)
+    assert mesh.watertight
 
 
 def test_uncertified_cells(vm, orc):
@@ -195,11 +156,8 @@ def lobe_masks(voxels=1024):
 def test_extract_precision_lattice_full_size(vm, orc, capsys):
     """The precision-stress lattice at its stated size: 512x512 sites with
     1e-6 jitter (near-cocircular quadruples everywhere), a 5-lobed occupancy.
-    Inside flags and the unsafe/overflow counts equal the oracle's. Every cell
-    equals the oracle's (labels exactly, vertices to 5e-7), or equals it once
-    zero-length edges are dropped, or is one of a few degenerate cells; a
-    sample of those agrees with the exact rational cell. The counts are
-    printed."""
+    Inside flags, the unsafe/overflow counts and every cell (labels and vertex
+    bits) equal the oracle's."""
     from voromesh_gb300 import OptimizerParams, VoroOptimizer, synth
 
     gen = np.ascontiguousarray(synth.lattice(1, 5, 512, 512, 1e-6).reshape(-1, 2))
@@ -215,36 +173,10 @@ def test_extract_precision_lattice_full_size(vm, orc, capsys):
         2.0, 2.0, masks, tiles, tiles, float(np.float32(1.0) / np.float32(voxel)), nthreads=8)
     assert np.array_equal(mesh.inside, inside) and inside.sum() > 50000
     assert mesh.unsafeCells == flags[0] and mesh.overflowCells == flags[1]
-    cs = np.asarray(mesh.cellStart)
-    cnt = np.diff(cs)
-    rows = np.repeat(np.arange(n), cnt)
-    cols = np.arange(cs[-1]) - np.repeat(cs[:-1], cnt)
-    lab = np.full((n, 24), -9999, np.int32)
-    ver = np.zeros((n, 24, 2), np.float32)
-    lab[rows, cols] = mesh.cellLabels
-    ver[rows, cols] = mesh.cellVerts
-    used = np.arange(24)[None, :] < counts[:, None]
-    ref = np.where(used, edges, -9999)
-    same = (cnt == counts) & np.all(lab == ref, axis=1)
-    vd = np.abs(ver - verts).max(axis=2)
-    assert np.where(used[same], vd[same], 0.0).max() <= 5e-7
-    zero_only, rest = 0, []
-    for i in np.nonzero(~same)[0]:
-        mine = drop_zero_edges(lab[i, :cnt[i]], ver[i, :cnt[i]])
-        theirs = drop_zero_edges(edges[i, :counts[i]], verts[i, :counts[i]])
-        if same_cycle(mine, theirs):
-            zero_only += 1
-        else:
-            rest.append(i)
-    for i in rest[:40]:
-        d = (gen[:, 0].astype(np.float64) - gen[i, 0]) ** 2 + (gen[:, 1].astype(np.float64) - gen[i, 1]) ** 2
-        exact = exact_cell(gen, i, np.argsort(d)[:48])
-        assert same_cycle(drop_zero_edges(lab[i, :cnt[i]], ver[i, :cnt[i]]), exact), f"cell {i}"
+    assert_cells_equal(mesh, n, verts, edges, counts)
     with capsys.disabled():
-        print(f"\nextraction, 512x512 jittered lattice: {int(same.sum())} cells equal, {zero_only} equal but for "
-              f"zero-length edges, {len(rest)} degenerate ({min(len(rest), 40)} checked exact); "
+        print(f"\nextraction, 512x512 jittered lattice: all {n} cells equal the oracle's bit for bit; "
               f"unsafe {mesh.unsafeCells}, watertight {mesh.watertight}")
-    assert len(rest) <= n // 100
 
 
 def test_extract_after_slot_grid_shrinks(vm):
