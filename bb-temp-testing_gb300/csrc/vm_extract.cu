@@ -33,37 +33,69 @@ struct CellPoly {
 };
 
 struct CellCtx {
-    float2 ci;
-    double w, h; // domain size
+    double cx, cy; // the cell's site, converted once
+    float fx, fy;  // and as given
+    double w, h;   // domain size
 };
 
-// 1 if vertex k is outside the half-plane <x, r> <= |r|^2/2 (reference clipByBisector :322-325)
-__device__ __forceinline__ bool outside(const CellPoly &P, int k, float rfx, float rfy, float cf, double rx, double ry,
-                                        double cc)
+// a - b is exact in float (Sterbenz: same sign and within a factor of 2, or
+// an operand zero), so it equals the exact difference rounded once, which is
+// also the FP64 difference rounded to float.
+__device__ __forceinline__ bool sub_exact(float a, float b)
 {
-    float a = P.fx[k] * rfx, b = P.fy[k] * rfy;
-    float f = a + b - cf;
-    float bound = 1.9073486328125e-06f * (fabsf(a) + fabsf(b) + cf + fabsf(f)) + 1e-37f; // 2^-19
-    if (f > bound) return true;
-    if (f < -bound) return false;
-    return P.vx[k] * rx + P.vy[k] * ry - cc > 0.0;
+    return a == 0.0f || b == 0.0f || (b > 0.0f ? (a >= 0.5f * b && a <= 2.0f * b) : (a <= 0.5f * b && a >= 2.0f * b));
 }
 
 // Clip P by the bisector of ci and site j (reference clipByBisector :320-351).
 // Writes into Q; returns false on vertex overflow. *changed = 0 if no vertex was outside.
+//
+// A vertex is outside the half-plane <x, r> <= |r|^2/2 (:322-325) when the
+// FP32 value of <x, r> - |r|^2/2 exceeds its error bound, inside when it is
+// below minus the bound; in between, the FP64 value decides. The FP64 offset
+// and half-norm are formed only when a vertex needs them or the polygon is
+// cut (the FP32 offset comes from the FP32 difference when that is exact).
 __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, float2 cj, bool &changed)
 {
-    double rx = (double)cj.x - (double)c.ci.x, ry = (double)cj.y - (double)c.ci.y;
-    double cc = 0.5 * (rx * rx + ry * ry);
-    float rfx = (float)rx, rfy = (float)ry;
+    double rx = 0.0, ry = 0.0, cc = 0.0;
+    bool have64 = false;
+    auto need64 = [&]() {
+        if (!have64) {
+            rx = (double)cj.x - c.cx;
+            ry = (double)cj.y - c.cy;
+            cc = 0.5 * (rx * rx + ry * ry);
+            have64 = true;
+        }
+    };
+    float rfx, rfy;
+    if (sub_exact(cj.x, c.fx) && sub_exact(cj.y, c.fy)) {
+        rfx = cj.x - c.fx;
+        rfy = cj.y - c.fy;
+    } else {
+        need64();
+        rfx = (float)rx;
+        rfy = (float)ry;
+    }
     float cf = 0.5f * (rfx * rfx + rfy * rfy);
-    unsigned out = 0;
-    for (int k = 0; k < P.n; ++k)
-        if (outside(P, k, rfx, rfy, cf, rx, ry, cc)) out |= 1u << k;
+    unsigned out = 0, band = 0;
+    for (int k = 0; k < P.n; ++k) {
+        float a = P.fx[k] * rfx, b = P.fy[k] * rfy;
+        float f = a + b - cf;
+        float bound = 1.9073486328125e-06f * (fabsf(a) + fabsf(b) + cf + fabsf(f)) + 1e-37f; // 2^-19
+        if (f > bound) out |= 1u << k;
+        else if (!(f < -bound)) band |= 1u << k;
+    }
+    if (band) {
+        need64();
+        for (unsigned m = band; m; m &= m - 1) {
+            int k = __ffs(m) - 1;
+            if (P.vx[k] * rx + P.vy[k] * ry - cc > 0.0) out |= 1u << k;
+        }
+    }
     if (!out) {
         changed = false;
         return true;
     }
+    need64();
     changed = true;
     bool ok = true;
     Q.n = 0;
@@ -161,12 +193,15 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
     }
 
     CellCtx c;
-    c.ci = ci;
+    c.cx = (double)ci.x;
+    c.cy = (double)ci.y;
+    c.fx = ci.x;
+    c.fy = ci.y;
     c.w = (double)F.width;
     c.h = (double)F.height;
     CellPoly buf[2];
     CellPoly *P = &buf[0], *Q = &buf[1];
-    double x0 = -(double)ci.x, y0 = -(double)ci.y, x1 = c.w - (double)ci.x, y1 = c.h - (double)ci.y;
+    double x0 = -c.cx, y0 = -c.cy, x1 = c.w - c.cx, y1 = c.h - c.cy;
     P->vx[0] = x0; P->vy[0] = y0; P->lab[0] = -1;
     P->vx[1] = x1; P->vy[1] = y0; P->lab[1] = -2;
     P->vx[2] = x1; P->vy[2] = y1; P->lab[2] = -3;
@@ -221,7 +256,7 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
                 for (int k = 0; k < kCellK; ++k) seen |= idx[k] == j;
                 if (seen) continue;
                 float2 g = F.sortedPos[s];
-                double rx = (double)g.x - (double)ci.x, ry = (double)g.y - (double)ci.y;
+                double rx = (double)g.x - c.cx, ry = (double)g.y - c.cy;
                 if (rx * rx + ry * ry > R2) continue;
                 if (nc == kGather) {
                     gathered = false;
@@ -239,7 +274,7 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
             for (int q = 0; q < nc; ++q) {
                 int j = cand[q];
                 float2 g = F.gen[j];
-                double rx = (double)g.x - (double)ci.x, ry = (double)g.y - (double)ci.y;
+                double rx = (double)g.x - c.cx, ry = (double)g.y - c.cy;
                 if (rx * rx + ry * ry > 4.0 * r2max_d(*P)) continue;
                 bool changed;
                 ok &= clip(c, *P, *Q, j, g, changed);
@@ -255,7 +290,7 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
             bool seen = false;
             for (int k = 0; k < kCellK; ++k) seen |= idx[k] == j;
             if (seen) continue;
-            double rx = (double)g.x - (double)ci.x, ry = (double)g.y - (double)ci.y;
+            double rx = (double)g.x - c.cx, ry = (double)g.y - c.cy;
             if (rx * rx + ry * ry > 4.0 * r2max_d(*P)) continue;
             bool changed;
             ok &= clip(c, *P, *Q, j, g, changed);
@@ -266,25 +301,30 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
     }
     if (!ok) atomicAdd(&flags[1], 1);
 
-    // centroid (shoelace) -> occupancy (reference :417-431)
-    double area = 0.0, cx = 0.0, cy = 0.0;
-    for (int k = 0; k < P->n; ++k) {
-        int k1 = k + 1 == P->n ? 0 : k + 1;
-        double ax = P->vx[k], ay = P->vy[k], bx = P->vx[k1], by = P->vy[k1];
-        double cr = ax * by - bx * ay;
-        area += cr;
-        cx += (ax + bx) * cr;
-        cy += (ay + by) * cr;
+    // centroid (shoelace) -> occupancy (reference :417-431); with no
+    // occupancy every cell is outside and the centroid is not needed
+    bool in = false;
+    if (masks) {
+        double area = 0.0, cx = 0.0, cy = 0.0;
+        for (int k = 0; k < P->n; ++k) {
+            int k1 = k + 1 == P->n ? 0 : k + 1;
+            double ax = P->vx[k], ay = P->vy[k], bx = P->vx[k1], by = P->vy[k1];
+            double cr = ax * by - bx * ay;
+            area += cr;
+            cx += (ax + bx) * cr;
+            cy += (ay + by) * cr;
+        }
+        float2 centroid = ci;
+        if (fabs(area) > 1e-12) {
+            centroid.x += (float)(cx / (3.0 * area));
+            centroid.y += (float)(cy / (3.0 * area));
+        }
+        in = occupied(masks, tilesX, tilesY, invVoxel, centroid);
     }
-    float2 centroid = ci;
-    if (fabs(area) > 1e-12) {
-        centroid.x += (float)(cx / (3.0 * area));
-        centroid.y += (float)(cy / (3.0 * area));
-    }
-    outInside[i] = occupied(masks, tilesX, tilesY, invVoxel, centroid) ? 1 : 0;
+    outInside[i] = in ? 1 : 0;
     outCount[i] = P->n;
     for (int k = 0; k < P->n; ++k) {
-        outVerts[(size_t)i * kMaxVerts + k] = make_float2((float)((double)ci.x + P->vx[k]), (float)((double)ci.y + P->vy[k]));
+        outVerts[(size_t)i * kMaxVerts + k] = make_float2((float)(c.cx + P->vx[k]), (float)(c.cy + P->vy[k]));
         outEdges[(size_t)i * kMaxVerts + k] = P->lab[k];
     }
 }
