@@ -48,13 +48,14 @@ __device__ __forceinline__ bool sub_exact(float a, float b)
 
 // Clip P by the bisector of ci and site j (reference clipByBisector :320-351).
 // Writes into Q; returns false on vertex overflow. *changed = 0 if no vertex was outside.
+// When it cuts, r2 = r2max_f(Q), taken as the vertices are written.
 //
 // A vertex is outside the half-plane <x, r> <= |r|^2/2 (:322-325) when the
 // FP32 value of <x, r> - |r|^2/2 exceeds its error bound, inside when it is
 // below minus the bound; in between, the FP64 value decides. The FP64 offset
 // and half-norm are formed only when a vertex needs them or the polygon is
 // cut (the FP32 offset comes from the FP32 difference when that is exact).
-__device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, float2 cj, bool &changed)
+__device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, float2 cj, bool &changed, float &r2)
 {
     double rx = 0.0, ry = 0.0, cc = 0.0;
     bool have64 = false;
@@ -99,15 +100,18 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
     changed = true;
     bool ok = true;
     Q.n = 0;
+    float r = 0.0f;
     for (int k = 0; k < P.n; ++k) {
         int k1 = k + 1 == P.n ? 0 : k + 1;
         bool inA = !((out >> k) & 1u), inB = !((out >> k1) & 1u);
         if (inA) {
             if (Q.n < kMaxVerts) {
+                const float fx = P.fx[k], fy = P.fy[k];
                 Q.vx[Q.n] = P.vx[k]; Q.vy[Q.n] = P.vy[k];
-                Q.fx[Q.n] = P.fx[k]; Q.fy[Q.n] = P.fy[k];
+                Q.fx[Q.n] = fx; Q.fy[Q.n] = fy;
                 Q.lab[Q.n] = P.lab[k];
                 ++Q.n;
+                r = fmaxf(r, fx * fx + fy * fy);
             } else ok = false;
         }
         if (inA != inB) {
@@ -117,13 +121,16 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
             const double t = fa / (fa - fb);
             const double x = ax + t * (bx - ax), y = ay + t * (by - ay);
             if (Q.n < kMaxVerts) {
+                const float fx = (float)x, fy = (float)y;
                 Q.vx[Q.n] = x; Q.vy[Q.n] = y;
-                Q.fx[Q.n] = (float)x; Q.fy[Q.n] = (float)y;
+                Q.fx[Q.n] = fx; Q.fy[Q.n] = fy;
                 Q.lab[Q.n] = inA ? j : P.lab[k];
                 ++Q.n;
+                r = fmaxf(r, fx * fx + fy * fy);
             } else ok = false;
         }
     }
+    r2 = r;
     return ok;
 }
 
@@ -142,9 +149,10 @@ __device__ __forceinline__ double r2max_d(const CellPoly &P)
 }
 
 // (double)dd > 4 * maxRadius2(P), decided in FP32 unless within its error band.
-__device__ __forceinline__ bool beyond(float dd, const CellPoly &P)
+// r4 = 4 * r2max_f(P), kept by the caller while P is unchanged.
+__device__ __forceinline__ bool beyond(float dd, const CellPoly &P, float r4)
 {
-    float r = 4.0f * r2max_f(P);
+    const float r = r4;
     if (dd > r * 1.0000038146972656f) return true;  // 1 + 2^-18
     if (dd < r * 0.9999961853027344f) return false; // 1 - 2^-18
     return (double)dd > 4.0 * r2max_d(P);
@@ -213,6 +221,7 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
     P->n = 4;
 
     bool ok = true, certified = false;
+    float r4 = 4.0f * r2max_f(*P); // refreshed after each cut
     for (int k = 0; k < kCellK; ++k) {
         int j = idx[k];
         if (j < 0) {
@@ -220,17 +229,19 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
             break;
         }
         if (j == i) continue;
-        if (beyond(d2[k], *P)) {
+        if (beyond(d2[k], *P, r4)) {
             certified = true;
             break;
         }
         bool changed;
-        ok &= clip(c, *P, *Q, j, F.gen[j], changed);
+        float r2;
+        ok &= clip(c, *P, *Q, j, F.gen[j], changed, r2);
         if (changed) {
             CellPoly *t = P; P = Q; Q = t;
+            r4 = 4.0f * r2;
         }
     }
-    if (!certified && beyond(d2[kCellK - 1], *P)) certified = true;
+    if (!certified && beyond(d2[kCellK - 1], *P, r4)) certified = true;
     if (!certified) {
         atomicAdd(&flags[0], 1);
         // The reference clips by every other generator in index order, skipping
@@ -277,7 +288,8 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
                 double rx = (double)g.x - c.cx, ry = (double)g.y - c.cy;
                 if (rx * rx + ry * ry > 4.0 * r2max_d(*P)) continue;
                 bool changed;
-                ok &= clip(c, *P, *Q, j, g, changed);
+                float r2;
+                ok &= clip(c, *P, *Q, j, g, changed, r2);
                 if (changed) {
                     CellPoly *t = P; P = Q; Q = t;
                 }
@@ -293,7 +305,8 @@ __global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, co
             double rx = (double)g.x - c.cx, ry = (double)g.y - c.cy;
             if (rx * rx + ry * ry > 4.0 * r2max_d(*P)) continue;
             bool changed;
-            ok &= clip(c, *P, *Q, j, g, changed);
+            float r2;
+            ok &= clip(c, *P, *Q, j, g, changed, r2);
             if (changed) {
                 CellPoly *t = P; P = Q; Q = t;
             }
