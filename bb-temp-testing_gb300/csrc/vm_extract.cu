@@ -170,7 +170,7 @@ __device__ __forceinline__ bool occupied(const unsigned long long *masks, int ti
     return (masks[(size_t)ty * tilesX + tx] >> (((j & 7) << 3) | (i & 7))) & 1ull;
 }
 
-__global__ void __launch_bounds__(128) k_cells(const VmFit *__restrict__ fit, const unsigned long long *masks,
+__global__ void __launch_bounds__(128, 7) k_cells(const VmFit *__restrict__ fit, const unsigned long long *masks,
                                                int tilesX, int tilesY, float invVoxel, float2 *__restrict__ outVerts,
                                                int *__restrict__ outEdges, int *__restrict__ outCount,
                                                unsigned char *__restrict__ outInside, int *__restrict__ flags)
