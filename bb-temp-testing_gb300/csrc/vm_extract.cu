@@ -115,7 +115,7 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
             } else ok = false;
         }
         if (inA != inB) {
-            // the reference's interpolation (:337-339); fa and fb differ in sign
+            // the reference's interpolation (:337-343); fa and fb differ in sign
             const double ax = P.vx[k], ay = P.vy[k], bx = P.vx[k1], by = P.vy[k1];
             const double fa = ax * rx + ay * ry - cc, fb = bx * rx + by * ry - cc;
             const double t = fa / (fa - fb);
