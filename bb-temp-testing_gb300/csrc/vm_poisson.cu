@@ -64,8 +64,9 @@ __device__ __forceinline__ void dart(float2 *grid, const PdParams &p, int cx, in
     if (cx >= 2 && cy >= 2 && cx < p.gridW - 2 && cy < p.gridH - 2) {
         // an interior cell: every neighbour is in the grid, and no address
         // depends on a loaded value, so the cell and its 8 nearest
-        // neighbours are loaded as one batch and the 16 at distance 2 as the
-        // next (the dart lands only if none conflicts, whatever the order)
+        // neighbours are loaded as one batch, then the 16 at distance 2 in
+        // batches of kBatch, each only if no earlier neighbour conflicts
+        // (the dart lands only if none conflicts, whatever the order)
         const int dxs[24] = {0, -1, 1, 0, -1, 1, -1, 1, 0, -2, 2, 0, -1, 1, -2, 2, -2, 2, -1, 1, -2, 2, -2, 2};
         const int dys[24] = {-1, 0, 0, 1, -1, -1, 1, 1, -2, 0, 0, 2, -2, -2, -1, -1, 1, 1, 2, 2, -2, -2, 2, 2};
         const float2 *c = grid + cellId;
