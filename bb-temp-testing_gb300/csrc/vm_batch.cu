@@ -100,6 +100,9 @@ struct BFit {
     VmFit desc{};
     VmPointSet sites{}, tset{};
     float2 *traw = nullptr;
+    // the live-target and 5x5-block counts are on their way to the host
+    // (hcounts); desc.nTargets, desc.fastShift and liveTargets wait for them
+    bool countsPending = false;
 };
 
 int fail_budget(const char *what) { return fail(VM_ERR_BUDGET, what); }
@@ -125,6 +128,7 @@ struct vmb_batch {
     bool dirty = true;
     std::vector<VmState> hostStates;
     DevBuf<int> block5Buf; // a fit's largest 5x5-block target count, read back at vmb_add_fit
+    int *hcounts = nullptr; // pinned, per fit id: live targets, largest 5x5-block count
     // pinned staging of host-to-device copies (a copy from pageable memory
     // would first wait for the stream); reused from its start after a sync
     char *hstage = nullptr;
@@ -163,6 +167,27 @@ cudaError_t stage_copy(vmb_batch *b, void *dst, const void *src, size_t bytes)
 // After a sync of the batch stream every staged copy has been read.
 void staging_done(vmb_batch *b) { b->hstageUsed = 0; }
 
+// Completes the fits added since the last sync: one stream sync for all of
+// them, then their live-target counts and fast-path shifts from hcounts.
+int resolve_counts(vmb_batch *b)
+{
+    bool any = false;
+    for (const BFit &f : b->fits) any |= f.live && f.countsPending;
+    if (!any) return VM_OK;
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e) return cuda_fail(e, "batch live targets");
+    staging_done(b);
+    for (int id = 0; id < (int)b->fits.size(); ++id) {
+        BFit &f = b->fits[id];
+        if (!f.live || !f.countsPending) continue;
+        f.liveTargets = b->hcounts[2 * id];
+        f.desc.nTargets = f.liveTargets;
+        f.desc.fastShift = vm_fast_shift(b->hcounts[2 * id + 1]);
+        f.countsPending = false;
+    }
+    return VM_OK;
+}
+
 int single_set_build(vmb_batch *b, const VmPointSet &S, int emptyIsNegative, int canonical)
 {
     VmPointSet T = S;
@@ -182,6 +207,8 @@ int single_set_build(vmb_batch *b, const VmPointSet &S, int emptyIsNegative, int
 
 int rebuild_tables(vmb_batch *b)
 {
+    int rc0 = resolve_counts(b);
+    if (rc0) return rc0;
     b->order.clear();
     for (int id = 0; id < (int)b->fits.size(); ++id)
         if (b->fits[id].live && !b->fits[id].done) b->order.push_back(id);
@@ -304,6 +331,10 @@ int vmb_create(size_t arenaBytes, int maxFits, int lossVariant, vmb_batch **out)
     if (!rc) rc = b->dOneFit.alloc(1);
     if (!rc) rc = b->dOneSet.alloc(1);
     if (!rc) rc = b->dOnePre.alloc(4);
+    if (!rc && (e = cudaMallocHost((void **)&b->hcounts, sizeof(int) * 2 * (size_t)maxFits))) {
+        b->hcounts = nullptr;
+        rc = cuda_fail(e, "batch counts");
+    }
     if (!rc && (e = cudaMemset(b->states.p, 0, sizeof(VmState) * maxFits))) rc = cuda_fail(e, "states");
     if (!rc) {
         b->lossVariant = (lossVariant >= 0 && lossVariant < vm_loss_variants()) ? lossVariant : 1;
@@ -328,6 +359,7 @@ int vmb_destroy(vmb_batch *b)
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
     if (b->hstage) cudaFreeHost(b->hstage);
+    if (b->hcounts) cudaFreeHost(b->hcounts);
     delete b;
     return VM_OK;
 }
@@ -507,25 +539,25 @@ int vmb_add_fit(vmb_batch *b, const vmb_fit *in, int *fitId)
         release_fit(b, f);
         return rc;
     }
-    int live = 0, b5 = 0;
     if ((rc = b->block5Buf.reserve(1))) {
         releaseTmp();
         release_fit(b, f);
         return rc;
     }
+    // the counts reach hcounts in stream order; the next table rebuild (or
+    // fit query) syncs once for every fit added since (resolve_counts). The
+    // temporary sort buffers go back to the arena now: whatever reuses them
+    // is enqueued on the same stream, after these copies.
+    int *slot = b->hcounts + 2 * id;
     if ((e = vm_launch_block5_max(f.tset.start, f.gridW, f.gridH, f.tset.sub, b->block5Buf.p, b->stream)) ||
-        (e = cudaMemcpyAsync(&live, liveAt, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
-        (e = cudaMemcpyAsync(&b5, b->block5Buf.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
-        (e = cudaStreamSynchronize(b->stream))) {
+        (e = cudaMemcpyAsync(slot, liveAt, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) ||
+        (e = cudaMemcpyAsync(slot + 1, b->block5Buf.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream))) {
         releaseTmp();
         release_fit(b, f);
         return cuda_fail(e, "vmb_add_fit live targets");
     }
-    staging_done(b);
     releaseTmp();
-    f.liveTargets = live;
-    D.nTargets = live;
-    D.fastShift = vm_fast_shift(b5);
+    f.countsPending = true;
     if ((rc = single_set_build(b, f.sites, 1, 1))) { // the grid of the initial generators
         release_fit(b, f);
         return rc;
@@ -602,7 +634,7 @@ int vmb_fit_info(vmb_batch *b, int fitId, vmb_fit_info_t *out)
     if (!b || !out || fitId < 0 || fitId >= (int)b->fits.size() || !b->fits[fitId].live)
         return fail(VM_ERR_ARG, "vmb_fit_info: no such fit");
     int rc;
-    if ((rc = read_states(b))) return rc;
+    if ((rc = resolve_counts(b)) || (rc = read_states(b))) return rc;
     const VmState &s = b->hostStates[fitId];
     out->iteration = s.iter;
     out->lastLoss = s.count > 0 ? s.loss / (float)s.count : 0.0f;
