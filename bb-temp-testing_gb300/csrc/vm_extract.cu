@@ -25,9 +25,11 @@ namespace vmk {
 constexpr int kMaxVerts = 24;
 constexpr int kCellK = 32;
 
+// A vertex's coordinates are stored as pairs, so that each is read and
+// written as one vector access of the thread's local memory.
 struct CellPoly {
-    double vx[kMaxVerts], vy[kMaxVerts];
-    float fx[kMaxVerts], fy[kMaxVerts];
+    double2 v[kMaxVerts]; // FP64 vertex, relative to the site
+    float2 f[kMaxVerts];  // the same rounded to FP32
     int lab[kMaxVerts];
     int n;
 };
@@ -79,7 +81,8 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
     float cf = 0.5f * (rfx * rfx + rfy * rfy);
     unsigned out = 0, band = 0;
     for (int k = 0; k < P.n; ++k) {
-        float a = P.fx[k] * rfx, b = P.fy[k] * rfy;
+        const float2 q = P.f[k];
+        float a = q.x * rfx, b = q.y * rfy;
         float f = a + b - cf;
         float bound = 1.9073486328125e-06f * (fabsf(a) + fabsf(b) + cf + fabsf(f)) + 1e-37f; // 2^-19
         if (f > bound) out |= 1u << k;
@@ -89,7 +92,8 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
         need64();
         for (unsigned m = band; m; m &= m - 1) {
             int k = __ffs(m) - 1;
-            if (P.vx[k] * rx + P.vy[k] * ry - cc > 0.0) out |= 1u << k;
+            const double2 v = P.v[k];
+            if (v.x * rx + v.y * ry - cc > 0.0) out |= 1u << k;
         }
     }
     if (!out) {
@@ -106,24 +110,25 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
         bool inA = !((out >> k) & 1u), inB = !((out >> k1) & 1u);
         if (inA) {
             if (Q.n < kMaxVerts) {
-                const float fx = P.fx[k], fy = P.fy[k];
-                Q.vx[Q.n] = P.vx[k]; Q.vy[Q.n] = P.vy[k];
-                Q.fx[Q.n] = fx; Q.fy[Q.n] = fy;
+                const float2 q = P.f[k];
+                Q.v[Q.n] = P.v[k];
+                Q.f[Q.n] = q;
                 Q.lab[Q.n] = P.lab[k];
                 ++Q.n;
-                r = fmaxf(r, fx * fx + fy * fy);
+                r = fmaxf(r, q.x * q.x + q.y * q.y);
             } else ok = false;
         }
         if (inA != inB) {
             // the reference's interpolation (:337-343); fa and fb differ in sign
-            const double ax = P.vx[k], ay = P.vy[k], bx = P.vx[k1], by = P.vy[k1];
+            const double2 va = P.v[k], vb = P.v[k1];
+            const double ax = va.x, ay = va.y, bx = vb.x, by = vb.y;
             const double fa = ax * rx + ay * ry - cc, fb = bx * rx + by * ry - cc;
             const double t = fa / (fa - fb);
             const double x = ax + t * (bx - ax), y = ay + t * (by - ay);
             if (Q.n < kMaxVerts) {
                 const float fx = (float)x, fy = (float)y;
-                Q.vx[Q.n] = x; Q.vy[Q.n] = y;
-                Q.fx[Q.n] = fx; Q.fy[Q.n] = fy;
+                Q.v[Q.n] = make_double2(x, y);
+                Q.f[Q.n] = make_float2(fx, fy);
                 Q.lab[Q.n] = inA ? j : P.lab[k];
                 ++Q.n;
                 r = fmaxf(r, fx * fx + fy * fy);
@@ -137,14 +142,20 @@ __device__ bool clip(const CellCtx &c, const CellPoly &P, CellPoly &Q, int j, fl
 __device__ __forceinline__ float r2max_f(const CellPoly &P)
 {
     float r = 0.0f;
-    for (int k = 0; k < P.n; ++k) r = fmaxf(r, P.fx[k] * P.fx[k] + P.fy[k] * P.fy[k]);
+    for (int k = 0; k < P.n; ++k) {
+        const float2 q = P.f[k];
+        r = fmaxf(r, q.x * q.x + q.y * q.y);
+    }
     return r;
 }
 
 __device__ __forceinline__ double r2max_d(const CellPoly &P)
 {
     double r = 0.0;
-    for (int k = 0; k < P.n; ++k) r = fmax(r, P.vx[k] * P.vx[k] + P.vy[k] * P.vy[k]);
+    for (int k = 0; k < P.n; ++k) {
+        const double2 v = P.v[k];
+        r = fmax(r, v.x * v.x + v.y * v.y);
+    }
     return r;
 }
 
@@ -210,13 +221,12 @@ __global__ void __launch_bounds__(128, 7) k_cells(const VmFit *__restrict__ fit,
     CellPoly buf[2];
     CellPoly *P = &buf[0], *Q = &buf[1];
     double x0 = -c.cx, y0 = -c.cy, x1 = c.w - c.cx, y1 = c.h - c.cy;
-    P->vx[0] = x0; P->vy[0] = y0; P->lab[0] = -1;
-    P->vx[1] = x1; P->vy[1] = y0; P->lab[1] = -2;
-    P->vx[2] = x1; P->vy[2] = y1; P->lab[2] = -3;
-    P->vx[3] = x0; P->vy[3] = y1; P->lab[3] = -4;
+    P->v[0] = make_double2(x0, y0); P->lab[0] = -1;
+    P->v[1] = make_double2(x1, y0); P->lab[1] = -2;
+    P->v[2] = make_double2(x1, y1); P->lab[2] = -3;
+    P->v[3] = make_double2(x0, y1); P->lab[3] = -4;
     for (int k = 0; k < 4; ++k) {
-        P->fx[k] = (float)P->vx[k];
-        P->fy[k] = (float)P->vy[k];
+        P->f[k] = make_float2((float)P->v[k].x, (float)P->v[k].y);
     }
     P->n = 4;
 
@@ -321,7 +331,8 @@ __global__ void __launch_bounds__(128, 7) k_cells(const VmFit *__restrict__ fit,
         double area = 0.0, cx = 0.0, cy = 0.0;
         for (int k = 0; k < P->n; ++k) {
             int k1 = k + 1 == P->n ? 0 : k + 1;
-            double ax = P->vx[k], ay = P->vy[k], bx = P->vx[k1], by = P->vy[k1];
+            const double2 va = P->v[k], vb = P->v[k1];
+            double ax = va.x, ay = va.y, bx = vb.x, by = vb.y;
             double cr = ax * by - bx * ay;
             area += cr;
             cx += (ax + bx) * cr;
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(128, 7) k_cells(const VmFit *__restrict__ fit,
     outInside[i] = in ? 1 : 0;
     outCount[i] = P->n;
     for (int k = 0; k < P->n; ++k) {
-        outVerts[(size_t)i * kMaxVerts + k] = make_float2((float)(c.cx + P->vx[k]), (float)(c.cy + P->vy[k]));
+        outVerts[(size_t)i * kMaxVerts + k] = make_float2((float)(c.cx + P->v[k].x), (float)(c.cy + P->v[k].y));
         outEdges[(size_t)i * kMaxVerts + k] = P->lab[k];
     }
 }
